@@ -1,0 +1,219 @@
+/*
+ * sphstokes.h — C ABI of libsphstokes, a GB300 (sm_103a) implementation of the
+ * pseudo-transient (PT) Stokes iteration of PTsolvers/SphericalStokes.
+ *
+ * The reference is a set of Julia scripts; its "interface" for the hot path is
+ * the sequence of ParallelStencil kernels launched inside the PT loop of each
+ * script (e.g. scripts_diapir/SphericalStokes_diapir.jl:409-443) and the
+ * arrays they mutate in place.  This library replaces that loop: the caller
+ * passes grid and physics parameters, the library owns the device arrays,
+ * runs the loop, and hands back converged P, velocities, stresses, effective
+ * viscosity and the error history.  Julia code binds it with `ccall`; arrays
+ * cross the boundary as plain `double*` in the reference's own column-major
+ * layout and sizes (so `pointer(A)` of a Julia Array{Float64,3} is passed
+ * as is).
+ *
+ * Conventions
+ *  - Every entry point returns int: 0 (SPH_OK) or a negative sph_status.
+ *    No exceptions or aborts cross the ABI; sph_strerror() names the code and
+ *    sph_last_error() gives the message of the last failure on this thread.
+ *  - A context is used by one host thread at a time.  All device work of a
+ *    context is issued on one CUDA stream (default: a stream the library
+ *    creates; sph_set_stream() installs the caller's).
+ *  - Index convention of fields: (ix,iy,iz) 1-based as in the reference,
+ *    ix fastest.  Field sizes are those of the reference's @zeros calls
+ *    (SphericalStokes_diapir.jl:381-399), see sph_field_dims().
+ */
+#ifndef SPHSTOKES_H
+#define SPHSTOKES_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+typedef enum sph_status {
+    SPH_OK = 0,
+    SPH_ERR_INVALID = -1,        /* bad argument or parameter */
+    SPH_ERR_CUDA = -2,           /* a CUDA call failed (message in sph_last_error) */
+    SPH_ERR_NOT_CONVERGED = -3,  /* maxiter reached before the tolerance */
+    SPH_ERR_DIVERGED = -4,       /* NaN/Inf in a norm (reference: error("NaN"), SphericalStokes_mxpu.jl:426) */
+    SPH_ERR_NOMEM = -5,          /* device or host allocation failed */
+    SPH_ERR_UNSUPPORTED = -6,    /* combination of options not implemented */
+    SPH_ERR_NO_DEVICE = -7       /* no CUDA device / the sm_103a kernels cannot run here */
+} sph_status;
+
+/* coordinate system: scripts_diapir/{Spherical,Cylindrical,Cartesian}Stokes_diapir.jl */
+typedef enum sph_geometry { SPH_GEOM_SPHERICAL = 0, SPH_GEOM_CYLINDRICAL = 1, SPH_GEOM_CARTESIAN = 2 } sph_geometry;
+
+/* arithmetic of the PT sweeps */
+typedef enum sph_precision {
+    SPH_PREC_FP64 = 0,  /* plain FP64 PT (the reference's Data.Number = Float64) */
+    SPH_PREC_FP32 = 1,  /* plain FP32 PT (storage and arithmetic) */
+    SPH_PREC_MIXED = 2  /* FP32 PT sweeps inside an FP64 defect-correction loop */
+} sph_precision;
+
+/* boundary-condition set */
+typedef enum sph_bc {
+    SPH_BC_DIAPIR = 0,     /* simple shear of the diapir scripts (sph: SphericalStokes_diapir.jl:61-99,
+                              cyl: CylindricalStokes_diapir.jl:358-366, cart: CartesianStokes_diapir.jl:371-379) */
+    SPH_BC_FREE_SLIP = 1,  /* free slip on all faces (SphericalStokes_plateau.jl:64-92); spherical only */
+    SPH_BC_STRESS = 2      /* free slip on the x1 faces, prescribed total normal stress sig_bc[1] on the x2
+                              faces and sig_bc[2] on the x3 faces (not in the reference); spherical only */
+} sph_bc;
+
+/* rheology update after the stress update */
+typedef enum sph_rheology {
+    SPH_RHEO_LINEAR = 0,           /* eta = eta_ini, no update */
+    SPH_RHEO_TAU_POWER = 1,        /* compute_TII! + power_law! (SphericalStokes_diapir.jl:243-265) */
+    SPH_RHEO_TAU_POWER_RELAX = 2,  /* the same with log-space relaxation of eta_PL
+                                      (CylindricalStokes_diapir.jl:185-192, CartesianStokes_diapir.jl:210-221) */
+    SPH_RHEO_EDOT_POWER_RELAX = 3  /* eta_t = 2/(1/eta_ini + 1/(eta_ini (edot_II/edot_bg)^((1-n)/n))),
+                                      eta <- eta^(1-relax) eta_t^relax (not in the reference) */
+} sph_rheology;
+
+/* initial state */
+typedef enum sph_init {
+    SPH_INIT_NONE = 0,       /* zeros; eta = eta_ini = eta0, rho = rho0; the caller sets fields */
+    SPH_INIT_INCLUSION = 1   /* initialize_inclusion! on rho and eta plus the shear initial velocity
+                                (SphericalStokes_diapir.jl:401-404 and the cyl/cart equivalents) */
+} sph_init;
+
+/* stopping criterion of sph_solve */
+typedef enum sph_criterion {
+    SPH_CRIT_REFERENCE = 0,  /* max_f max|V_f - V_f(previous iteration)| / max|V_f| < tol and iter > 20
+                                (SphericalStokes_diapir.jl:427-439) */
+    SPH_CRIT_RESIDUAL = 1    /* FP64 Stokes residual: max(max|R_mom|/f_scale, max|div V| l1/max|V|) < tol */
+} sph_criterion;
+
+typedef enum sph_field {
+    SPH_FIELD_P = 0,
+    SPH_FIELD_V1 = 1,      /* VR / VR / VX   (n1+1, n2, n3) */
+    SPH_FIELD_V2 = 2,      /* Vθ / Vθ / VY   (n1, n2+1, n3) */
+    SPH_FIELD_V3 = 3,      /* Vφ / VZ / VZ   (n1, n2, n3+1) */
+    SPH_FIELD_TAU11 = 4,   /* τ_RR           (n1, n2, n3) */
+    SPH_FIELD_TAU22 = 5,
+    SPH_FIELD_TAU33 = 6,
+    SPH_FIELD_TAU12 = 7,   /* τ_Rθ           (n1-1, n2-1, n3-2) */
+    SPH_FIELD_TAU13 = 8,   /* τ_Rφ           (n1-1, n2-2, n3-1) */
+    SPH_FIELD_TAU23 = 9,   /* τ_θφ           (n1-2, n2-1, n3-1) */
+    SPH_FIELD_ETA = 10,    /* effective viscosity η */
+    SPH_FIELD_ETA_INI = 11,
+    SPH_FIELD_ETA_SM = 12, /* ηSM = local 7-point maximum of η */
+    SPH_FIELD_DT_R = 13,   /* velocity pseudo-time step */
+    SPH_FIELD_TII = 14,    /* second invariant of τ */
+    SPH_FIELD_RHO = 15,
+    SPH_FIELD_PHASE = 16,  /* 1 = linear cell for the power laws, 0 = power law (values 0/1 as double) */
+    SPH_FIELD_ETA_PL = 17, /* η_PL state of SPH_RHEO_TAU_POWER_RELAX */
+    SPH_FIELD_COUNT = 18
+} sph_field;
+
+/* grid, physics and PT parameters.  sph_params_default() fills the values of
+ * the reference script of the given geometry (e.g. SphericalStokes_diapir.jl:348-367). */
+typedef struct sph_params {
+    int32_t abi_version;   /* = SPH_ABI_VERSION */
+    int32_t geometry;      /* sph_geometry */
+    int32_t precision;     /* sph_precision */
+    int32_t bc;            /* sph_bc */
+    int32_t rheology;      /* sph_rheology */
+    int32_t init;          /* sph_init */
+    int32_t n1, n2, n3;    /* cells (P nodes) along x1, x2, x3 = nr, nθ, nφ (or nz / nx, ny, nz) */
+    double c1, c2, c3;     /* domain centre: (r, π/2, 0) sph, (r, 0, 0) cyl, (0, 0, 0) cart */
+    double l1, l2, l3;     /* domain lengths: (lr, lθ, lφ) etc.; node coordinates span c ± l/2 */
+    double l_ref;          /* length in KBDT/GSDT (lr, or lx in Cartesian) */
+    double vpdt;           /* PT step length: dr*CFL in the reference (:400) */
+    double dmp;            /* damping parameter (:10) */
+    double g;              /* gravity (radial for sph/cyl, along x3 for cart) */
+    double tau_C;          /* characteristic stress of the stress power laws */
+    double n_exp;          /* power-law exponent */
+    double n_exp_late;     /* exponent switched to once the error drops below switch_err (cyl script :342-344) */
+    double switch_err;     /* 0 disables the switch */
+    double relax;          /* relaxation factor of the relaxed laws */
+    double edot_bg;        /* background strain rate of SPH_RHEO_EDOT_POWER_RELAX */
+    double r;              /* sphere / cylinder radius used by the shear BCs and the inclusion test */
+    double sh;             /* shearing velocity of the diapir BCs */
+    double sig_bc[3];      /* SPH_BC_STRESS: prescribed total normal stress on the x1 (unused), x2, x3 faces */
+    /* SPH_INIT_INCLUSION */
+    double eta0, vr;       /* matrix viscosity; inclusion viscosity = eta0 / vr */
+    double rho0, rho_in;   /* matrix and inclusion density */
+    double radius;         /* compared with the SQUARED distance, as the reference does (:132) */
+    int32_t incl_linear;   /* 1: inclusion cells are linear (phase = 1) */
+    int32_t reserved0;
+    double reserved[8];
+} sph_params;
+
+/* solve controls and result */
+typedef struct sph_solve_opts {
+    int32_t criterion;     /* sph_criterion */
+    int32_t nout;          /* check every nout iterations (reference: 100) */
+    int64_t maxiter;       /* cap on PT iterations (all precisions; inner sweeps in MIXED) */
+    double tol;            /* stopping tolerance (reference: 5e-7 on the velocity change) */
+    /* MIXED only */
+    double inner_rtol;     /* inner FP32 sweeps stop when their residual drops by this factor */
+    int32_t max_outer;     /* cap on FP64 defect-correction steps */
+    int32_t inner_max;     /* cap on FP32 sweeps per correction step */
+    double warm_tol;       /* FP32 nonlinear warm start runs to this FP64 residual first (0 = skip) */
+    double reserved[6];
+} sph_solve_opts;
+
+typedef struct sph_solve_info {
+    int64_t iters;         /* PT iterations done (FP32 + FP64 sweeps) */
+    int32_t outer;         /* defect-correction steps (MIXED) */
+    int32_t status;        /* sph_status of the solve */
+    double err;            /* final error of the chosen criterion */
+    double residual;       /* final FP64 residual (SPH_CRIT_RESIDUAL definition) */
+    double seconds;        /* wall time of the solve */
+    int64_t nhist;         /* entries written to hist_iter / hist_err */
+} sph_solve_info;
+
+/* defaults of the reference script of the given geometry (diapir setups) */
+int sph_params_default(sph_params* p, int32_t geometry);
+
+/* sizes (reference layout) of a field: dims[0..2] */
+int sph_field_dims(const sph_params* p, int32_t field, int64_t dims[3]);
+
+/* allocate device state, build coordinate tables, apply p->init */
+int sph_create(const sph_params* p, void** ctx);
+int sph_destroy(void* ctx);
+
+/* run device work of this context on `stream` (a cudaStream_t); NULL restores the library's own */
+int sph_set_stream(void* ctx, void* stream);
+
+/* copy a field from / to host memory in the reference layout (count = product of sph_field_dims) */
+int sph_set_field(void* ctx, int32_t field, const double* host, int64_t count);
+int sph_get_field(void* ctx, int32_t field, double* host, int64_t count);
+
+/* exactly k reference PT iterations (equal3! ... BC_φ!, SphericalStokes_diapir.jl:413-425) */
+int sph_step(void* ctx, int64_t k);
+
+/* iterate to the tolerance; hist_* (may be NULL) receive up to hist_cap (iter, err) pairs */
+int sph_solve(void* ctx, const sph_solve_opts* opts, sph_solve_info* info,
+              int64_t* hist_iter, double* hist_err, int64_t hist_cap);
+
+/* FP64 Stokes residual of the current state: out[0..2] max|R_mom| per component,
+ * out[3] max|div V|, out[4] max|V|, out[5] f_scale, out[6] the SPH_CRIT_RESIDUAL error */
+int sph_residual(void* ctx, double out[7]);
+
+/* single reference kernels on the context's state (per-kernel parity):
+ * maxloc!+copy_BC!(ηSM), compute_P!, compute_TII!+copy_BC!(τII), power_law!/rheology,
+ * compute_V!, BC_R!/BC_θ!/BC_φ! (all stages of the BC set) */
+typedef enum sph_kernel {
+    SPH_K_MAXLOC = 0, SPH_K_COMPUTE_P = 1, SPH_K_RHEOLOGY = 2, SPH_K_COMPUTE_V = 3, SPH_K_BC = 4
+} sph_kernel;
+int sph_run_kernel(void* ctx, int32_t kernel);
+
+/* device time (ms) of the last sph_step / sph_solve call measured with CUDA events */
+int sph_last_device_ms(void* ctx, double* ms);
+
+const char* sph_strerror(int code);
+const char* sph_last_error(void);
+int sph_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPHSTOKES_H */

@@ -1,0 +1,198 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper of ``oracle/_build/liboracle.so``, the FP64 CPU restatement of
+the reference's PT kernels (``oracle/oracle.cpp``).  Only ``tests/``,
+``__graft_entry__.smoke()`` and ``bench.py``'s CPU baseline / reference arm
+use it, as the checker; the product library never calls it.
+
+Arrays are numpy float64 in the reference's layout: Fortran order, the sizes of
+the scripts' ``@zeros`` calls, ``A[i,j,k]`` = Julia ``A[i+1,j+1,k+1]``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from pathlib import Path
+
+import numpy as np
+
+_DIR = Path(__file__).resolve().parent
+LIB_PATH = _DIR / "_build" / "liboracle.so"
+PI = 3.141592653589793
+_PD = C.POINTER(C.c_double)
+_PU8 = C.POINTER(C.c_uint8)
+
+
+class SphState(C.Structure):
+    _fields_ = [("nr", C.c_int64), ("nt", C.c_int64), ("np", C.c_int64)] + [
+        (n, _PD) for n in ("P", "VR", "Vt", "Vp", "VR_err", "Vt_err", "Vp_err", "tRR", "ttt", "tpp", "tRt", "tRp",
+                           "ttp", "rho", "eta", "eta_ini", "etaSM", "DT_R", "tII", "R", "th", "ph")
+    ] + [("phase", _PU8), ("eta_tmp", _PD)]
+
+
+class SphParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("_dr", "_dt", "_dp", "dmp", "vpdt", "lr", "g", "tau_C", "n_exp", "r", "sh")] + [
+        ("bc", C.c_int32), ("rheo", C.c_int32)] + [(n, C.c_double) for n in ("relax", "edot_bg", "sig_t", "sig_p")]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            from sphericalstokes_gb300.build import build_oracle
+            build_oracle()
+        L = C.CDLL(str(LIB_PATH))
+        L.orc_sph_iterate.argtypes = [C.POINTER(SphState), C.POINTER(SphParams), C.c_int64]
+        L.orc_sph_check_err.argtypes = [C.POINTER(SphState)]
+        L.orc_sph_check_err.restype = C.c_double
+        L.orc_sph_equal3.argtypes = [C.POINTER(SphState)]
+        for n in ("orc_sph_compute_P", "orc_sph_power_law", "orc_sph_compute_V", "orc_sph_apply_bc"):
+            getattr(L, n).argtypes = [C.POINTER(SphState), C.POINTER(SphParams)]
+        L.orc_sph_compute_TII.argtypes = [C.POINTER(SphState)]
+        L.orc_copy_BC.argtypes = [_PD, C.c_int64, C.c_int64, C.c_int64]
+        L.orc_copy_boundary_faces.argtypes = [_PD, C.c_int64, C.c_int64, C.c_int64]
+        L.orc_maxloc.argtypes = [_PD, _PD, C.c_int64, C.c_int64, C.c_int64]
+        L.orc_sph_edot_law.argtypes = [C.POINTER(SphState), C.POINTER(SphParams), _PD, C.c_int32, _PD]
+        L.orc_sph_scratch_size.argtypes = [C.c_int64] * 3
+        L.orc_sph_scratch_size.restype = C.c_int64
+        L.orc_sph_residual.argtypes = [C.POINTER(SphState), C.POINTER(SphParams), _PD, _PD, _PD, _PD, _PD, _PD]
+        L.orc_sph_residual_scratch_size.argtypes = [C.c_int64] * 3
+        L.orc_sph_residual_scratch_size.restype = C.c_int64
+        L.orc_num_threads.restype = C.c_int32
+        L.orc_set_num_threads.argtypes = [C.c_int32]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(_PD) if a is not None else None
+
+
+def linspace(c: float, l: float, n: int) -> np.ndarray:
+    """Node coordinates c - l/2 .. c + l/2 (the reference's range(a, b, length=n)); same formula as the library."""
+    lo, hi = c - l / 2.0, c + l / 2.0
+    x = np.array([lo + (hi - lo) * i / (n - 1) for i in range(n)], dtype=np.float64)
+    x[-1] = hi
+    return x
+
+
+class Sph:
+    """State of one spherical solve (SphericalStokes_diapir.jl:369-404) held in numpy arrays."""
+
+    NAMES = {"P": "P", "V1": "VR", "V2": "Vt", "V3": "Vp", "TAU11": "tRR", "TAU22": "ttt", "TAU33": "tpp",
+             "TAU12": "tRt", "TAU13": "tRp", "TAU23": "ttp", "ETA": "eta", "ETA_INI": "eta_ini", "ETA_SM": "etaSM",
+             "DT_R": "DT_R", "TII": "tII", "RHO": "rho"}
+
+    def __init__(self, nr, nt, np_, *, r, c2, lr, lt, lp, l_ref, dmp, vpdt, g, tau_C, n_exp, sh, bc, rheo,
+                 relax=0.5, edot_bg=1.0, sig_t=0.0, sig_p=0.0, c1=None, c3=0.0):
+        self.n = (nr, nt, np_)
+        c1 = r if c1 is None else c1
+        z = lambda *s: np.zeros(s, dtype=np.float64, order="F")
+        self.P = z(nr, nt, np_); self.VR = z(nr + 1, nt, np_); self.Vt = z(nr, nt + 1, np_); self.Vp = z(nr, nt, np_ + 1)
+        self.VR_err = z(nr + 1, nt, np_); self.Vt_err = z(nr, nt + 1, np_); self.Vp_err = z(nr, nt, np_ + 1)
+        self.tRR = z(nr, nt, np_); self.ttt = z(nr, nt, np_); self.tpp = z(nr, nt, np_)
+        self.tRt = z(nr - 1, nt - 1, np_ - 2); self.tRp = z(nr - 1, nt - 2, np_ - 1); self.ttp = z(nr - 2, nt - 1, np_ - 1)
+        self.rho = z(nr, nt, np_); self.eta = z(nr, nt, np_) + 1.0; self.eta_ini = z(nr, nt, np_)
+        self.etaSM = z(nr, nt, np_); self.DT_R = z(nr, nt, np_); self.tII = z(nr, nt, np_)
+        x1, x2, x3 = linspace(c1, lr, nr), linspace(c2, lt, nt), linspace(c3, lp, np_)
+        self.x1, self.x2, self.x3 = x1, x2, x3
+        self.R = np.asfortranarray(np.broadcast_to(x1[:, None, None], (nr, nt, np_)).copy())
+        self.th = np.asfortranarray(np.broadcast_to(x2[None, :, None], (nr, nt, np_)).copy())
+        self.ph = np.asfortranarray(np.broadcast_to(x3[None, None, :], (nr, nt, np_)).copy())
+        self.phase = np.zeros((nr, nt, np_), dtype=np.uint8, order="F")
+        self.eta_tmp = np.zeros(nr * nt * np_ + int(lib().orc_sph_scratch_size(nr, nt, np_)), dtype=np.float64)
+        self.prm = SphParams(_dr=(nr - 1) / lr, _dt=(nt - 1) / lt, _dp=(np_ - 1) / lp, dmp=dmp, vpdt=vpdt, lr=l_ref,
+                             g=g, tau_C=tau_C, n_exp=n_exp, r=r, sh=sh, bc=bc, rheo=rheo, relax=relax,
+                             edot_bg=edot_bg, sig_t=sig_t, sig_p=sig_p)
+        self._sync()
+
+    def _sync(self):
+        s = SphState(nr=self.n[0], nt=self.n[1], np=self.n[2])
+        for f, _ in SphState._fields_[3:-2]:
+            setattr(s, f, _ptr(getattr(self, f)))
+        s.phase = self.phase.ctypes.data_as(_PU8)
+        s.eta_tmp = _ptr(self.eta_tmp)
+        self.st = s
+
+    @classmethod
+    def from_params(cls, p) -> "Sph":
+        """Oracle state for a library ``Params`` (spherical geometry), initialised like the library."""
+        rheo = {0: 2, 1: 0, 3: 1}[p.rheology]
+        o = cls(p.n1, p.n2, p.n3, r=p.r, c1=p.c1, c2=p.c2, c3=p.c3, lr=p.l1, lt=p.l2, lp=p.l3, l_ref=p.l_ref,
+                dmp=p.dmp, vpdt=p.vpdt if p.vpdt > 0 else p.l1 / (p.n1 - 1) / (2.0 + 4.5 * math.log10(p.vr)),
+                g=p.g, tau_C=p.tau_C, n_exp=p.n_exp, sh=p.sh, bc=p.bc, rheo=rheo, relax=p.relax,
+                edot_bg=p.edot_bg, sig_t=p.sig_bc[1], sig_p=p.sig_bc[2])
+        o.rho[:] = p.rho0
+        o.eta[:] = p.eta0
+        if p.init == 1:
+            L = lib()
+            L.orc_sph_init_inclusion.argtypes = [_PD, _PD, _PD, _PD, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double]
+            L.orc_sph_init_velocity.argtypes = [_PD, _PD, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double]
+            nr, nt, np_ = o.n
+            L.orc_sph_init_inclusion(_ptr(o.rho), _ptr(o.R), _ptr(o.th), _ptr(o.ph), nr, nt, np_, p.r, p.radius, p.rho_in)
+            L.orc_sph_init_inclusion(_ptr(o.eta), _ptr(o.R), _ptr(o.th), _ptr(o.ph), nr, nt, np_, p.r, p.radius, p.eta0 / p.vr)
+            L.orc_sph_init_velocity(_ptr(o.Vp), _ptr(o.th), nr, nt, np_, p.sh, p.r)
+            if p.incl_linear:
+                o.phase[:] = (o.eta != p.eta0).astype(np.uint8)
+        o.eta_ini[:] = o.eta
+        return o
+
+    def field(self, name: str) -> np.ndarray:
+        return getattr(self, self.NAMES[name])
+
+    # kernels
+    def iterate(self, k: int = 1):
+        lib().orc_sph_iterate(C.byref(self.st), C.byref(self.prm), int(k))
+
+    def equal3(self):
+        lib().orc_sph_equal3(C.byref(self.st))
+
+    def check_err(self) -> float:
+        return float(lib().orc_sph_check_err(C.byref(self.st)))
+
+    def maxloc(self):
+        nr, nt, np_ = self.n
+        lib().orc_maxloc(_ptr(self.etaSM), _ptr(self.eta), nr, nt, np_)
+        lib().orc_copy_BC(_ptr(self.etaSM), nr, nt, np_)
+
+    def compute_P(self):
+        lib().orc_sph_compute_P(C.byref(self.st), C.byref(self.prm))
+
+    def power_law(self):
+        nr, nt, np_ = self.n
+        L = lib()
+        if self.prm.rheo == 0:
+            L.orc_sph_compute_TII(C.byref(self.st))
+            L.orc_copy_BC(_ptr(self.tII), nr, nt, np_)
+            L.orc_sph_power_law(C.byref(self.st), C.byref(self.prm))
+        elif self.prm.rheo == 1:
+            out = np.zeros_like(self.eta)
+            L.orc_sph_edot_law(C.byref(self.st), C.byref(self.prm), _ptr(out), 1, _ptr(self.eta_tmp))
+            self.eta[:] = out
+
+    def compute_V(self):
+        lib().orc_sph_compute_V(C.byref(self.st), C.byref(self.prm))
+
+    def apply_bc(self):
+        lib().orc_sph_apply_bc(C.byref(self.st), C.byref(self.prm))
+
+    def residual(self, f_scale: float | None = None) -> dict:
+        nr, nt, np_ = self.n
+        scr = np.zeros(int(lib().orc_sph_residual_scratch_size(nr, nt, np_)), dtype=np.float64)
+        out = np.zeros(5, dtype=np.float64)
+        lib().orc_sph_residual(C.byref(self.st), C.byref(self.prm), _ptr(out), _ptr(scr), None, None, None, None)
+        fs = f_scale if f_scale is not None else max(np.abs(self.rho).max() * abs(self.prm.g), 1e-300)
+        mom = out[:3].max() / fs
+        cont = out[3] * (self.x1[-1] - self.x1[0]) / (out[4] if out[4] > 0 else 1.0)
+        return {"mom1": out[0], "mom2": out[1], "mom3": out[2], "div": out[3], "vmax": out[4], "err": max(mom, cont)}
+
+
+def set_threads(n: int):
+    lib().orc_set_num_threads(int(n))
+
+
+def num_threads() -> int:
+    return int(lib().orc_num_threads())

@@ -1,0 +1,582 @@
+// Pseudo-transient kernels (one thread per grid point, direct global access).
+//
+// These are the building blocks of one PT iteration in the reference's order
+// (SphericalStokes_diapir.jl:413-425):
+//   k_maxloc   maxloc! + copy_BC!(ηSM)          :149-152, :102-124
+//   k_stress   compute_P!                        :155-241
+//   k_rheo_tau compute_TII! + copy_BC!(τII) + power_law!   :243-265
+//   k_strain / k_edot_law   strain-rate power law (not in the reference)
+//   k_velocity compute_V!                        :267-329
+//   k_bc       BC_R! / BC_θ! / BC_φ! and the cyl/cart BC kernels
+// All three coordinate systems share the kernels; the metric terms come from
+// the template parameter G and the 1D tables in Geo.  The FP32 fused sweep in
+// sph_fused.cuh implements the same arithmetic with shared-memory tiling.
+#pragma once
+#include "sph_common.cuh"
+
+namespace sph {
+
+// ---------------------------------------------------------------------------
+// ηSM = 7-point maximum of η on interior cells; boundary cells take the value
+// of the clamped interior cell (copy_bc_r!, copy_bc_θ!, copy_bc_φ! in that
+// order leave exactly that).  faces_only: CartesianStokes_diapir.jl:97-105
+// copies only face interiors and edges/corners keep η (ηSM .= η before maxloc!).
+template <typename T>
+__global__ void k_maxloc(KP<T> p, int faces_only) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int c = i + d.sy * j + d.sz * k;
+    int nb = (i == 0 || i == d.n1 - 1) + (j == 0 || j == d.n2 - 1) + (k == 0 || k == d.n3 - 1);
+    if (faces_only && nb >= 2) { p.etaSM[c] = p.eta[c]; return; }
+    const int a = clampi(i, 1, d.n1 - 2), b = clampi(j, 1, d.n2 - 2), e = clampi(k, 1, d.n3 - 2);
+    const int s = a + d.sy * b + d.sz * e;
+    const T* E = p.eta;
+    p.etaSM[c] = jmax(jmax(jmax(jmax(E[s - 1], E[s + 1]), E[s]), jmax(E[s - d.sy], E[s + d.sy])), jmax(E[s - d.sz], E[s + d.sz]));
+}
+
+// ---------------------------------------------------------------------------
+// compute_P!: pressure, normal deviatoric stresses and DT_R at cells, shear
+// stresses at edges.  RHS: continuity right-hand side rP (correction problem:
+// P -= KBDT*(div δV + div V_fp64)).
+template <typename T, int G, bool RHS>
+__global__ void __launch_bounds__(256) k_stress(KP<T> p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const T h = T(0.5), q4 = T(0.25);
+    {
+        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
+        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
+        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
+        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
+        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
+        T D11, D22, D33;
+        if (G != CART) {
+            const T t3 = div * T(1.0 / 3.0);
+            D11 = p.d1 * d1v - t3;
+            D22 = m.a2 * d2v + m.e1 * avx - t3;
+            D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
+        } else {
+            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
+        }
+        const T sm = p.etaSM[c], e = p.eta[c];
+        const T gs = p.gsc * sm, kb = p.kbc * sm;
+        const T f = e / (e + gs);  // 1/(1 + GSDT/η)
+        T dv = div;
+        if (RHS) dv += p.rP[c];
+        p.P[c] = p.P[c] - kb * dv;
+        p.t11[c] = (p.t11[c] + T(2) * gs * D11) * f;
+        p.t22[c] = (p.t22[c] + T(2) * gs * D22) * f;
+        p.t33[c] = (p.t33[c] + T(2) * gs * D33) * f;
+        p.DT_R[c] = p.vpdt2 / (kb + gs * f);
+    }
+    // τ12 at (i+1/2, j+1/2, k+1): cells (i|i+1, j|j+1, k+1)
+    if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
+        const int q = c + sz;
+        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sy] + p.etaSM[q + 1] + p.etaSM[q + 1 + sy]) * q4);
+        const T aE = (p.eta[q] + p.eta[q + sy] + p.eta[q + 1] + p.eta[q + 1 + sy]) * q4;
+        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1];   // V2 (i, j+1, k+1), (i+1, j+1, k+1)
+        const T v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];    // V1 (i+1, j, k+1), (i+1, j+1, k+1)
+        T D;
+        if (G != CART) {
+            const T iR = p.geo.invRh[i];
+            D = (v2b - v2a) * p.d1 + iR * (v1b - v1a) * p.d2 - (v2a + v2b) * h * iR;
+        } else {
+            D = (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
+        }
+        p.t12[c] = (p.t12[c] + aG * D) * (aE / (aE + aG));
+    }
+    // τ13 at (i+1/2, j+1, k+1/2): cells (i|i+1, j+1, k|k+1)
+    if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
+        const int q = c + sy;
+        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + 1] + p.etaSM[q + 1 + sz]) * q4);
+        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + 1] + p.eta[q + 1 + sz]) * q4;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1];   // V3 (i, j+1, k+1), (i+1, j+1, k+1)
+        const T v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];    // V1 (i+1, j+1, k), (i+1, j+1, k+1)
+        T D;
+        if (G == SPH) {
+            const T iR = p.geo.invRh[i];
+            D = (v3b - v3a) * p.d1 + iR * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * iR;
+        } else {
+            D = (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
+        }
+        p.t13[c] = (p.t13[c] + aG * D) * (aE / (aE + aG));
+    }
+    // τ23 at (i+1, j+1/2, k+1/2): cells (i+1, j|j+1, k|k+1)
+    if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
+        const int q = c + 1;
+        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + sy] + p.etaSM[q + sy + sz]) * q4);
+        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + sy] + p.eta[q + sy + sz]) * q4;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy];  // V3 (i+1, j, k+1), (i+1, j+1, k+1)
+        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];  // V2 (i+1, j+1, k), (i+1, j+1, k+1)
+        T D;
+        if (G == SPH) {
+            const T iR = p.geo.invRc[i + 1];
+            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
+        } else if (G == CYL) {
+            const T iR = p.geo.invRc[i + 1];
+            D = iR * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        } else {
+            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        }
+        p.t23[c] = (p.t23[c] + aG * D) * (aE / (aE + aG));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// second invariant of τ at an interior cell s (compute_TII!, :246-255)
+template <typename T>
+__device__ __forceinline__ T tau_II(const KP<T>& p, int s) {
+    const int sy = p.d.sy, sz = p.d.sz;
+    const T q4 = T(0.25);
+    const int e = s - 1 - sy - sz;  // edge (I-1, J-1, K-1)
+    const T a = (p.t12[e] + p.t12[e + sy] + p.t12[e + 1] + p.t12[e + 1 + sy]) * q4;
+    const T b = (p.t13[e] + p.t13[e + sz] + p.t13[e + 1] + p.t13[e + 1 + sz]) * q4;
+    const T c = (p.t23[e] + p.t23[e + sz] + p.t23[e + sy] + p.t23[e + sy + sz]) * q4;
+    const T x = p.t11[s], y = p.t22[s], z = p.t33[s];
+    return sqrt(T(0.5) * (x * x + y * y + z * z) + a * a + b * b + c * c);
+}
+
+// compute_TII! + copy_BC!(τII) + power_law! (RELAX: log-space relaxation of
+// η_PL, CylindricalStokes_diapir.jl:185-192).  phase==1 cells are linear.
+template <typename T, bool RELAX>
+__global__ void k_rheo_tau(KP<T> p, int faces_only, T n_exp) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int c = i + d.sy * j + d.sz * k;
+    const int nb = (i == 0 || i == d.n1 - 1) + (j == 0 || j == d.n2 - 1) + (k == 0 || k == d.n3 - 1);
+    T tii;
+    if (faces_only && nb >= 2) {
+        tii = p.tII[c];  // CartesianStokes_diapir.jl:97-105 never writes edges/corners of τII
+    } else {
+        const int s = clampi(i, 1, d.n1 - 2) + d.sy * clampi(j, 1, d.n2 - 2) + d.sz * clampi(k, 1, d.n3 - 2);
+        tii = tau_II(p, s);
+        p.tII[c] = tii;
+    }
+    const T ne = (p.phase && p.phase[c]) ? T(1) : n_exp;
+    const T ei = p.eta_ini[c];
+    if (!RELAX) {
+        p.eta[c] = T(2) / (T(1) / ei + T(1) / (ei * pow(tii / p.tau_C, T(1) - ne)));
+    } else {
+        T pl = ei * pow(tii / p.tau_C, T(1) - ne);
+        pl = exp(log(pl) * p.relax + log(p.eta_pl[c]) * (T(1) - p.relax));
+        p.eta_pl[c] = pl;
+        p.eta[c] = T(2) / (T(1) / ei + T(1) / pl);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// strain rates of the current velocities (as compute_P! forms them):
+// sDD = 0.5*(D11^2 + D22^2 + D33^2) at cells, s12/s13/s23 = engineering shear
+// strain rates at the edges.
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_strain(KP<T> p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const T h = T(0.5);
+    {
+        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
+        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
+        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
+        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
+        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
+        T D11, D22, D33;
+        if (G != CART) {
+            const T t3 = div * T(1.0 / 3.0);
+            D11 = p.d1 * d1v - t3; D22 = m.a2 * d2v + m.e1 * avx - t3; D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
+        } else {
+            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
+        }
+        p.sDD[c] = h * (D11 * D11 + D22 * D22 + D33 * D33);
+    }
+    if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
+        const int q = c + sz;
+        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];
+        p.s12[c] = (G != CART) ? (v2b - v2a) * p.d1 + p.geo.invRh[i] * (v1b - v1a) * p.d2 - (v2a + v2b) * h * p.geo.invRh[i]
+                               : (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
+    }
+    if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
+        const int q = c + sy;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];
+        p.s13[c] = (G == SPH) ? (v3b - v3a) * p.d1 + p.geo.invRh[i] * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * p.geo.invRh[i]
+                              : (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
+    }
+    if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
+        const int q = c + 1;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy], v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];
+        T D;
+        if (G == SPH) {
+            const T iR = p.geo.invRc[i + 1];
+            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
+        } else if (G == CYL) {
+            D = p.geo.invRc[i + 1] * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        } else {
+            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        }
+        p.s23[c] = D;
+    }
+}
+
+// strain-rate power law (not in the reference): the invariant of the clamped
+// interior cell (as copy_BC! does for τII), η_t = 2/(1/η_ini + 1/η_PL),
+// η_PL = η_ini (edot_II/edot_bg)^((1-n)/n); RELAXED: η_out = η^(1-relax) η_t^relax.
+template <typename T, bool RELAXED>
+__global__ void k_edot_law(KP<T> p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const int s = clampi(i, 1, d.n1 - 2) + sy * clampi(j, 1, d.n2 - 2) + sz * clampi(k, 1, d.n3 - 2);
+    const T q4 = T(0.25);
+    const int e = s - 1 - sy - sz;
+    const T a = (p.s12[e] + p.s12[e + sy] + p.s12[e + 1] + p.s12[e + 1 + sy]) * q4;
+    const T b = (p.s13[e] + p.s13[e + sz] + p.s13[e + 1] + p.s13[e + 1 + sz]) * q4;
+    const T cc = (p.s23[e] + p.s23[e + sz] + p.s23[e + sy] + p.s23[e + sy + sz]) * q4;
+    const T ed = sqrt(p.sDD[s] + q4 * (a * a + b * b + cc * cc));
+    const T ei = p.eta_ini[c];
+    T et;
+    if (p.phase && p.phase[c]) {
+        et = ei;
+    } else {
+        const T pl = ei * pow(ed / p.edot_bg, (T(1) - p.n_exp) / p.n_exp);
+        et = T(2) / (T(1) / ei + T(1) / pl);
+    }
+    p.eta_out[c] = RELAXED ? exp((T(1) - p.relax) * log(p.eta[c]) + p.relax * log(et)) : et;
+}
+
+// ---------------------------------------------------------------------------
+// compute_V!: momentum residuals at interior velocity nodes (:267-307).
+// GRAV: include the ρg body force; RHS: add the right-hand side rV instead.
+// ok[f] tells whether (I,J,K) is an interior node of velocity component f.
+template <typename T, int G, bool GRAV, bool RHS>
+__device__ __forceinline__ void momentum(const KP<T>& p, int I, int J, int K, T dv[3], bool ok[3]) {
+    const Dims& d = p.d;
+    const int sy = d.sy, sz = d.sz;
+    const int c = I + sy * J + sz * K;
+    const T h = T(0.5);
+    const T Pc = p.P[c];
+    const T s11 = p.t11[c] - Pc, s22 = p.t22[c] - Pc, s33 = p.t33[c] - Pc;
+    ok[0] = (J <= d.n2 - 2 && K <= d.n3 - 2);
+    ok[1] = (I <= d.n1 - 2 && K <= d.n3 - 2);
+    ok[2] = (I <= d.n1 - 2 && J <= d.n2 - 2);
+    // V1 (I-1/2, J, K)
+    if (ok[0]) {
+        const int m = c - 1;
+        const T Pm = p.P[m];
+        const T s11m = p.t11[m] - Pm, s22m = p.t22[m] - Pm, s33m = p.t33[m] - Pm;
+        const T ta = p.t12[m - sz], tb = p.t12[m - sy - sz];       // τ12 (I-1, J, K-1), (I-1, J-1, K-1)
+        const T ua = p.t13[m - sy], ub = p.t13[m - sy - sz];       // τ13 (I-1, J-1, K), (I-1, J-1, K-1)
+        T r;
+        if (G == SPH) {
+            const T iR = p.geo.invRh[I - 1], iS = p.geo.invSinC[J], ct = p.geo.cotC[J];
+            r = (s11 - s11m) * p.d1 + iR * (ta - tb) * p.d2 + iR * iS * (ua - ub) * p.d3 +
+                (T(2) * ((s11m + s11) * h) - (((s22m + s22) * h) + ((s33m + s33) * h))) * iR + ((tb + ta) * h) * iR * ct;
+        } else if (G == CYL) {
+            const T iR = p.geo.invRh[I - 1];
+            r = (s11 - s11m) * p.d1 + iR * (ta - tb) * p.d2 + (ua - ub) * p.d3 + (((s11m + s11) * h) - ((s22m + s22) * h)) * iR;
+        } else {
+            r = (s11 - s11m) * p.d1 + (ta - tb) * p.d2 + (ua - ub) * p.d3;
+        }
+        if (G != CART && GRAV) r -= (p.rho[m] * p.g + p.rho[c] * p.g) * h;
+        if (RHS) r += p.rV1[c];
+        dv[0] = r;
+    }
+    // V2 (I, J-1/2, K)
+    if (ok[1]) {
+        const int m = c - sy;
+        const T Pm = p.P[m];
+        const T s22m = p.t22[m] - Pm, s33m = p.t33[m] - Pm;
+        const T ta = p.t12[c - sy - sz], tb = p.t12[c - 1 - sy - sz];  // τ12 (I, J-1, K-1), (I-1, J-1, K-1)
+        const T ua = p.t23[c - 1 - sy], ub = p.t23[c - 1 - sy - sz];   // τ23 (I-1, J-1, K), (I-1, J-1, K-1)
+        T r;
+        if (G == SPH) {
+            const T iR = p.geo.invRc[I], iS = p.geo.invSinH[J - 1], ct = p.geo.cotH[J - 1];
+            r = (ta - tb) * p.d1 + iR * (s22 - s22m) * p.d2 + iR * iS * (ua - ub) * p.d3 + T(3) * ((tb + ta) * h) * iR +
+                (((s22m + s22) * h) - ((s33m + s33) * h)) * iR * ct;
+        } else if (G == CYL) {
+            const T iR = p.geo.invRc[I];
+            r = (ta - tb) * p.d1 + iR * (s22 - s22m) * p.d2 + (ua - ub) * p.d3 + T(2) * ((tb + ta) * h) * iR;
+        } else {
+            r = (ta - tb) * p.d1 + (s22 - s22m) * p.d2 + (ua - ub) * p.d3;
+        }
+        if (RHS) r += p.rV2[c];
+        dv[1] = r;
+    }
+    // V3 (I, J, K-1/2)
+    if (ok[2]) {
+        const int m = c - sz;
+        const T s33m = p.t33[m] - p.P[m];
+        const T ta = p.t13[c - sy - sz], tb = p.t13[c - 1 - sy - sz];  // τ13 (I, J-1, K-1), (I-1, J-1, K-1)
+        const T ua = p.t23[c - 1 - sz], ub = p.t23[c - 1 - sy - sz];   // τ23 (I-1, J, K-1), (I-1, J-1, K-1)
+        T r;
+        if (G == SPH) {
+            const T iR = p.geo.invRc[I], iS = p.geo.invSinC[J], ct = p.geo.cotC[J];
+            r = (ta - tb) * p.d1 + iR * (ua - ub) * p.d2 + iR * iS * (s33 - s33m) * p.d3 + T(3) * ((tb + ta) * h) * iR +
+                T(2) * ((ub + ua) * h) * iR * ct;
+        } else if (G == CYL) {
+            const T iR = p.geo.invRc[I];
+            r = (ta - tb) * p.d1 + iR * (ua - ub) * p.d2 + (s33 - s33m) * p.d3 + ((tb + ta) * h) * iR;
+        } else {
+            r = (ta - tb) * p.d1 + (ua - ub) * p.d2 + (s33 - s33m) * p.d3;
+        }
+        if (G == CART && GRAV) r -= p.g * (h * (p.rho[m] + p.rho[c]));
+        if (RHS) r += p.rV3[c];
+        dv[2] = r;
+    }
+}
+
+// MODE 0: V += dV*avg(DT_R) with the ρg body force (reference compute_V!)
+// MODE 1: V += (dV + rV)*avg(DT_R), no gravity (correction problem)
+// MODE 2: rV = dV with gravity (residual evaluation, V unchanged)
+template <typename T, int G, int MODE>
+__global__ void __launch_bounds__(256) k_velocity(KP<T> p) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1, K = blockIdx.z + 1;
+    const Dims& d = p.d;
+    if (I > d.n1 - 1 || J > d.n2 - 1 || K > d.n3 - 1) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = I + sy * J + sz * K;
+    T dv[3];
+    bool ok[3];
+    momentum<T, G, MODE != 1, MODE == 1>(p, I, J, K, dv, ok);
+    const T h = T(0.5);
+    if (MODE == 2) {
+        if (ok[0]) p.rV1[c] = dv[0];
+        if (ok[1]) p.rV2[c] = dv[1];
+        if (ok[2]) p.rV3[c] = dv[2];
+    } else {
+        if (ok[0]) p.V1[c] = p.V1[c] + dv[0] * ((p.DT_R[c - 1] + p.DT_R[c]) * h);
+        if (ok[1]) p.V2[c] = p.V2[c] + dv[1] * ((p.DT_R[c - sy] + p.DT_R[c]) * h);
+        if (ok[2]) p.V3[c] = p.V3[c] + dv[2] * ((p.DT_R[c - sz] + p.DT_R[c]) * h);
+    }
+}
+
+// max |dV + rV| of the correction problem into red[0] (inner stopping test)
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_velocity_norm(KP<T> p) {
+    const int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1, K = blockIdx.z + 1;
+    const Dims& d = p.d;
+    double m = 0.0;
+    if (I <= d.n1 - 1 && J <= d.n2 - 1 && K <= d.n3 - 1) {
+        T dv[3];
+        bool ok[3];
+        momentum<T, G, false, true>(p, I, J, K, dv, ok);
+        for (int f = 0; f < 3; ++f)
+            if (ok[f]) {
+                double x = fabs((double)dv[f]);
+                m = fmax(m, x != x ? (double)INFINITY : x);
+            }
+    }
+    // block reduction over the 2D block
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ double sm[32];
+    const int t = threadIdx.x + blockDim.x * threadIdx.y;
+    const int lane = t & 31, w = t >> 5, nw = (blockDim.x * blockDim.y) >> 5;
+    if (lane == 0) sm[w] = m;
+    __syncthreads();
+    if (w == 0) {
+        m = lane < nw ? sm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) atomicMax(p.red, ord_bits(m));
+    }
+}
+
+// viscous stresses of the current velocities: τ_ii = 2 η D_ii at cells,
+// τ_ij = avg4(η) D_ij at edges (the PT stress update's fixed point), and
+// rP = div V.  Used by the FP64 residual.
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_tau_visc(KP<T> p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const T h = T(0.5), q4 = T(0.25);
+    {
+        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
+        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
+        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
+        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
+        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
+        T D11, D22, D33;
+        if (G != CART) {
+            const T t3 = div * T(1.0 / 3.0);
+            D11 = p.d1 * d1v - t3; D22 = m.a2 * d2v + m.e1 * avx - t3; D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
+        } else {
+            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
+        }
+        const T e2 = T(2) * p.eta[c];
+        p.t11[c] = e2 * D11; p.t22[c] = e2 * D22; p.t33[c] = e2 * D33;
+        p.rP[c] = div;
+    }
+    if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
+        const int q = c + sz;
+        const T aE = (p.eta[q] + p.eta[q + sy] + p.eta[q + 1] + p.eta[q + 1 + sy]) * q4;
+        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];
+        const T D = (G != CART) ? (v2b - v2a) * p.d1 + p.geo.invRh[i] * (v1b - v1a) * p.d2 - (v2a + v2b) * h * p.geo.invRh[i]
+                                : (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
+        p.t12[c] = aE * D;
+    }
+    if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
+        const int q = c + sy;
+        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + 1] + p.eta[q + 1 + sz]) * q4;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];
+        const T D = (G == SPH) ? (v3b - v3a) * p.d1 + p.geo.invRh[i] * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * p.geo.invRh[i]
+                               : (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
+        p.t13[c] = aE * D;
+    }
+    if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
+        const int q = c + 1;
+        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + sy] + p.eta[q + sy + sz]) * q4;
+        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy], v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];
+        T D;
+        if (G == SPH) {
+            const T iR = p.geo.invRc[i + 1];
+            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
+        } else if (G == CYL) {
+            D = p.geo.invRc[i + 1] * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        } else {
+            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
+        }
+        p.t23[c] = aE * D;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions.  A BC set is a list of stages run in order; the ops of
+// one stage act on different fields across the faces normal to one axis, so
+// they are independent.  Each op writes both faces of its field:
+//   NEG     A[b] = -A[in]          COPY  A[b] = A[in]          ZERO  A[b] = 0
+//   LIN     A[b] = (x_cd - c1)*c0  LIN2M A[b] = 2*(x_cd - c1)*c0 - A[in]
+//   STRESS  normal-velocity ghost giving the boundary cell the total normal
+//           stress sig (x2 or x3 faces; not in the reference)
+// x_cd is the cell-centre coordinate of the node along axis cd.  In the
+// homogeneous form (correction problem) constants vanish: LIN -> 0,
+// LIN2M -> -A[in], sig -> 0.
+enum BcKind { BC_NEG = 0, BC_COPY = 1, BC_ZERO = 2, BC_LIN = 3, BC_LIN2M = 4, BC_STRESS = 5 };
+struct BcOp { int field; int kind; int cd; double c0, c1; };
+struct BcStage { int dim; int nops; BcOp op[3]; };
+
+template <typename T>
+__device__ __forceinline__ T* vfield(const KP<T>& p, int f) { return f == 0 ? p.V1 : (f == 1 ? p.V2 : p.V3); }
+
+template <typename T, int G>
+__global__ void k_bc(KP<T> p, BcStage st, int homog) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
+    const Dims& d = p.d;
+    const int D = st.dim;
+    const int sy = d.sy, sz = d.sz;
+    for (int o = 0; o < st.nops; ++o) {
+        const BcOp op = st.op[o];
+        const int f = op.field;
+        // extents of field f: V1 (n1+1,n2,n3), V2 (n1,n2+1,n3), V3 (n1,n2,n3+1)
+        int ext[3] = {d.n1 + (f == 0), d.n2 + (f == 1), d.n3 + (f == 2)};
+        const int du = D == 0 ? 1 : 0, dv = D == 2 ? 1 : 2;
+        if (u >= ext[du] || v >= ext[dv]) continue;
+        T* A = vfield(p, f);
+        const int stride[3] = {1, sy, sz};
+        const int base = u * stride[du] + v * stride[dv];
+        for (int side = 0; side < 2; ++side) {
+            const int b = side == 0 ? 0 : ext[D] - 1;
+            const int in = side == 0 ? 1 : ext[D] - 2;
+            const int cb = base + b * stride[D], ci = base + in * stride[D];
+            T val;
+            switch (op.kind) {
+                case BC_NEG: val = -A[ci]; break;
+                case BC_COPY: val = A[ci]; break;
+                case BC_ZERO: val = T(0); break;
+                case BC_LIN: {
+                    if (homog) { val = T(0); break; }
+                    const int idx = (op.cd == D) ? b : (op.cd == du ? u : v);
+                    const T* xc = op.cd == 0 ? p.geo.x1c : (op.cd == 1 ? p.geo.x2c : p.geo.x3c);
+                    val = (xc[idx] - T(op.c1)) * T(op.c0);
+                    break;
+                }
+                case BC_LIN2M: {
+                    if (homog) { val = -A[ci]; break; }
+                    const int idx = (op.cd == D) ? b : (op.cd == du ? u : v);
+                    const T* xc = op.cd == 0 ? p.geo.x1c : (op.cd == 1 ? p.geo.x2c : p.geo.x3c);
+                    val = T(2) * (xc[idx] - T(op.c1)) * T(op.c0) - A[ci];
+                    break;
+                }
+                default: {  // BC_STRESS on V2 (D == 1) or V3 (D == 2)
+                    const int cellb = side == 0 ? 0 : ext[D] - 2;        // boundary cell index along D
+                    const int cc = base + cellb * stride[D];             // boundary cell
+                    const int i = (D == 0) ? cellb : u;
+                    const int j = (D == 1) ? cellb : (du == 1 ? u : v);
+                    const CellMetric<T> m = cell_metric<T, G>(p, i, j);
+                    const T sig = homog ? T(0) : (D == 1 ? p.sig2 : p.sig3);
+                    const T sgn = side == 0 ? T(-1) : T(1);
+                    const T avx = (p.V1[cc] + p.V1[cc + 1]) * T(0.5);
+                    const T vin = A[ci];
+                    const T Dt = (sig + p.P[cc]) / (T(2) * p.eta[cc]);
+                    T A0, B, C0, Cg;
+                    if (D == 1) {
+                        A0 = p.d1 * (p.V1[cc + 1] - p.V1[cc]) + m.a3 * (p.V3[cc + sz] - p.V3[cc]) + m.c1 * avx + m.a2 * (-sgn) * vin + m.c2 * T(0.5) * vin;
+                        B = m.a2 * sgn + T(0.5) * m.c2;
+                        C0 = m.a2 * (-sgn) * vin + m.e1 * avx - A0 / T(3);
+                        Cg = m.a2 * sgn - B / T(3);
+                    } else {
+                        const T avy = (p.V2[cc] + p.V2[cc + sy]) * T(0.5);
+                        A0 = p.d1 * (p.V1[cc + 1] - p.V1[cc]) + m.a2 * (p.V2[cc + sy] - p.V2[cc]) + m.c1 * avx + m.c2 * avy + m.a3 * (-sgn) * vin;
+                        B = m.a3 * sgn;
+                        C0 = m.a3 * (-sgn) * vin + m.e1b * avx + m.e2 * avy - A0 / T(3);
+                        Cg = m.a3 * sgn - B / T(3);
+                    }
+                    val = (Dt - C0) / Cg;
+                    break;
+                }
+            }
+            A[cb] = val;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reductions: max|a| (or max|a-b|) over n entries into red[slot]
+// block-wide max of non-negative values (NaN mapped to +inf by the caller),
+// one atomicMax per block on the order-preserving bits
+__device__ __forceinline__ void block_max_to(double v, unsigned long long* slot) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double sm[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) atomicMax(slot, ord_bits(v));
+    }
+}
+
+template <typename T>
+__global__ void k_maxabs(const T* __restrict__ a, const T* __restrict__ b, long long n, unsigned long long* slot) {
+    double m = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        double x = b ? (double)a[q] - (double)b[q] : (double)a[q];
+        x = fabs(x);
+        m = fmax(m, (x != x) ? (double)INFINITY : x);
+    }
+    block_max_to(m, slot);
+}
+
+// ---------------------------------------------------------------------------
+// elementwise helpers over the whole box
+template <typename TD, typename TS>
+__global__ void k_convert(TD* __restrict__ dst, const TS* __restrict__ src, long long n) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) dst[q] = (TD)src[q];
+}
+// dst += (double)src
+template <typename TS>
+__global__ void k_add_widen(double* __restrict__ dst, const TS* __restrict__ src, long long n) {
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) dst[q] += (double)src[q];
+}
+
+}  // namespace sph

@@ -1,0 +1,998 @@
+// libsphstokes — C ABI over the sm_103a pseudo-transient Stokes kernels.
+//
+// The context owns the device arrays of one grid (FP64 master state, plus an
+// FP32 state for the FP32 / mixed-precision paths), the metric tables and the
+// boundary-condition program, and drives the PT loop of the reference scripts
+// (SphericalStokes_diapir.jl:409-443) on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "sph_pt.cuh"
+#include "sphstokes.h"
+
+using namespace sph;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            return fail(SPH_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));        \
+        }                                                                                         \
+    } while (0)
+
+const double kPi = 3.141592653589793;
+
+enum FieldSlot {
+    F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23,
+    F_ETA, F_ETA_INI, F_ETA_SM, F_DT_R, F_TII, F_RHO, F_ETA_PL, F_ETA_OUT,
+    F_V1E, F_V2E, F_V3E, F_RP, F_RV1, F_RV2, F_RV3, F_SDD, F_S12, F_S13, F_S23,
+    F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23,
+    F_NSLOTS
+};
+
+template <typename T>
+struct State {
+    T* f[F_NSLOTS] = {};
+    T* slab = nullptr;
+    T* tab = nullptr;  // metric tables
+    Geo<T> geo{};
+};
+
+struct Ctx {
+    sph_params prm;
+    Dims d;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    State<double> s64;
+    State<float> s32;
+    bool has32 = false;
+    bool stale32 = true;   // FP32 state must be refreshed from FP64 before use
+    bool stale64 = false;  // FP64 state must be refreshed from FP32 before use
+    uint8_t* phase = nullptr;
+    unsigned long long* red = nullptr;   // device reduction slots
+    unsigned long long* hred = nullptr;  // pinned host copy
+    std::vector<BcStage> bc;
+    double cur_n = 1.0;
+    double f_scale = 1.0;
+    double last_ms = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::vector<double> hx1, hx2, hx3;  // node coordinates (host)
+};
+
+constexpr int kRedSlots = 16;
+
+int field_extent(const Dims& d, int f, int e[3]) {
+    e[0] = d.n1; e[1] = d.n2; e[2] = d.n3;
+    switch (f) {
+        case SPH_FIELD_V1: e[0] += 1; break;
+        case SPH_FIELD_V2: e[1] += 1; break;
+        case SPH_FIELD_V3: e[2] += 1; break;
+        case SPH_FIELD_TAU12: e[0] -= 1; e[1] -= 1; e[2] -= 2; break;
+        case SPH_FIELD_TAU13: e[0] -= 1; e[1] -= 2; e[2] -= 1; break;
+        case SPH_FIELD_TAU23: e[0] -= 2; e[1] -= 1; e[2] -= 1; break;
+        default: break;
+    }
+    return 0;
+}
+
+int slot_of(int field) {
+    switch (field) {
+        case SPH_FIELD_P: return F_P;
+        case SPH_FIELD_V1: return F_V1;
+        case SPH_FIELD_V2: return F_V2;
+        case SPH_FIELD_V3: return F_V3;
+        case SPH_FIELD_TAU11: return F_T11;
+        case SPH_FIELD_TAU22: return F_T22;
+        case SPH_FIELD_TAU33: return F_T33;
+        case SPH_FIELD_TAU12: return F_T12;
+        case SPH_FIELD_TAU13: return F_T13;
+        case SPH_FIELD_TAU23: return F_T23;
+        case SPH_FIELD_ETA: return F_ETA;
+        case SPH_FIELD_ETA_INI: return F_ETA_INI;
+        case SPH_FIELD_ETA_SM: return F_ETA_SM;
+        case SPH_FIELD_DT_R: return F_DT_R;
+        case SPH_FIELD_TII: return F_TII;
+        case SPH_FIELD_RHO: return F_RHO;
+        case SPH_FIELD_ETA_PL: return F_ETA_PL;
+        default: return -1;
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <typename T>
+KP<T> make_kp(Ctx& c, State<T>& s) {
+    KP<T> p;
+    std::memset(&p, 0, sizeof(p));
+    const sph_params& q = c.prm;
+    p.d = c.d;
+    p.geo = s.geo;
+    p.P = s.f[F_P]; p.V1 = s.f[F_V1]; p.V2 = s.f[F_V2]; p.V3 = s.f[F_V3];
+    p.t11 = s.f[F_T11]; p.t22 = s.f[F_T22]; p.t33 = s.f[F_T33]; p.t12 = s.f[F_T12]; p.t13 = s.f[F_T13]; p.t23 = s.f[F_T23];
+    p.eta = s.f[F_ETA]; p.eta_ini = s.f[F_ETA_INI]; p.etaSM = s.f[F_ETA_SM]; p.DT_R = s.f[F_DT_R]; p.tII = s.f[F_TII];
+    p.rho = s.f[F_RHO]; p.eta_pl = s.f[F_ETA_PL]; p.eta_out = s.f[F_ETA_OUT];
+    p.phase = c.phase;
+    p.rP = s.f[F_RP]; p.rV1 = s.f[F_RV1]; p.rV2 = s.f[F_RV2]; p.rV3 = s.f[F_RV3];
+    p.sDD = s.f[F_SDD]; p.s12 = s.f[F_S12]; p.s13 = s.f[F_S13]; p.s23 = s.f[F_S23];
+    p.d1 = T((q.n1 - 1) / q.l1); p.d2 = T((q.n2 - 1) / q.l2); p.d3 = T((q.n3 - 1) / q.l3);
+    p.kbc = T(q.dmp * 2.0 * kPi * q.vpdt / q.l_ref);
+    p.gsc = T(4.0 * kPi * q.vpdt / q.l_ref);
+    p.vpdt2 = T(q.vpdt * q.vpdt);
+    p.g = T(q.g);
+    p.tau_C = T(q.tau_C); p.n_exp = T(c.cur_n); p.relax = T(q.relax); p.edot_bg = T(q.edot_bg);
+    p.sig2 = T(q.sig_bc[1]); p.sig3 = T(q.sig_bc[2]);
+    p.red = c.red;
+    return p;
+}
+
+dim3 blk2d() { return dim3(32, 8, 1); }
+dim3 grid_cells(const Dims& d) { return dim3((d.n1 + 31) / 32, (d.n2 + 7) / 8, d.n3); }
+dim3 grid_vel(const Dims& d) { return dim3((d.n1 - 1 + 31) / 32, (d.n2 - 1 + 7) / 8, d.n3 - 1); }
+
+int ew_blocks(long long n) { return (int)std::min<long long>((n + 255) / 256, 152LL * 16); }
+
+// ---------------------------------------------------------------------------
+// boundary-condition programs (the reference's BC kernels in call order)
+BcOp op(int field, int kind, int cd = 0, double c0 = 0.0, double c1 = 0.0) {
+    BcOp o; o.field = field; o.kind = kind; o.cd = cd; o.c0 = c0; o.c1 = c1;
+    return o;
+}
+BcStage stage(int dim, std::initializer_list<BcOp> ops) {
+    BcStage s; std::memset(&s, 0, sizeof(s));
+    s.dim = dim; s.nops = 0;
+    for (const BcOp& o : ops) s.op[s.nops++] = o;
+    return s;
+}
+
+int build_bc(Ctx& c) {
+    const sph_params& q = c.prm;
+    c.bc.clear();
+    const double rsh = q.r * q.sh;
+    if (q.bc == SPH_BC_FREE_SLIP) {  // SphericalStokes_plateau.jl:64-92
+        c.bc.push_back(stage(0, {op(0, BC_NEG), op(1, BC_COPY), op(2, BC_COPY)}));
+        c.bc.push_back(stage(1, {op(0, BC_COPY), op(1, BC_NEG), op(2, BC_COPY)}));
+        c.bc.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY), op(2, BC_NEG)}));
+        return SPH_OK;
+    }
+    if (q.bc == SPH_BC_STRESS) {
+        if (q.geometry == SPH_GEOM_CARTESIAN) return fail(SPH_ERR_UNSUPPORTED, "SPH_BC_STRESS needs a deviatoric (spherical or cylindrical) scheme");
+        c.bc.push_back(stage(0, {op(0, BC_NEG), op(1, BC_COPY), op(2, BC_COPY)}));
+        c.bc.push_back(stage(1, {op(0, BC_COPY), op(2, BC_COPY)}));
+        c.bc.push_back(stage(1, {op(1, BC_STRESS)}));
+        c.bc.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY)}));
+        c.bc.push_back(stage(2, {op(2, BC_STRESS)}));
+        return SPH_OK;
+    }
+    if (q.bc != SPH_BC_DIAPIR) return fail(SPH_ERR_INVALID, "unknown bc");
+    switch (q.geometry) {
+        case SPH_GEOM_SPHERICAL:  // SphericalStokes_diapir.jl:61-99
+            c.bc.push_back(stage(0, {op(0, BC_NEG), op(1, BC_COPY), op(2, BC_COPY)}));
+            c.bc.push_back(stage(1, {op(0, BC_ZERO), op(1, BC_NEG), op(2, BC_LIN, 1, rsh, kPi / 2.0)}));
+            c.bc.push_back(stage(2, {op(0, BC_ZERO), op(1, BC_ZERO), op(2, BC_LIN2M, 1, rsh, kPi / 2.0)}));
+            break;
+        case SPH_GEOM_CYLINDRICAL:  // CylindricalStokes_diapir.jl:358-366
+            c.bc.push_back(stage(0, {op(2, BC_COPY), op(1, BC_COPY), op(0, BC_NEG)}));
+            c.bc.push_back(stage(1, {op(2, BC_LIN, 1, rsh, 0.0), op(0, BC_ZERO), op(1, BC_NEG)}));
+            c.bc.push_back(stage(2, {op(1, BC_ZERO), op(0, BC_ZERO), op(2, BC_LIN2M, 1, rsh, 0.0)}));
+            break;
+        case SPH_GEOM_CARTESIAN:  // CartesianStokes_diapir.jl:371-379
+            c.bc.push_back(stage(0, {op(0, BC_LIN2M, 1, q.sh, 0.0), op(1, BC_ZERO), op(2, BC_ZERO)}));
+            c.bc.push_back(stage(1, {op(0, BC_LIN, 1, q.sh, 0.0), op(1, BC_NEG), op(2, BC_ZERO)}));
+            c.bc.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY), op(2, BC_NEG)}));
+            break;
+        default: return fail(SPH_ERR_INVALID, "unknown geometry");
+    }
+    return SPH_OK;
+}
+
+template <typename T, int G>
+void launch_bc(Ctx& c, KP<T>& p, int homog) {
+    for (const BcStage& st : c.bc) {
+        int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1;
+        int ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
+        dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
+        k_bc<T, G><<<g, blk2d(), 0, c.stream>>>(p, st, homog);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// allocation and set-up
+template <typename T>
+int alloc_state(Ctx& c, State<T>& s) {
+    const long long vol = c.d.vol;
+    CK(cudaMalloc((void**)&s.slab, sizeof(T) * vol * F_NSLOTS));
+    CK(cudaMemsetAsync(s.slab, 0, sizeof(T) * vol * F_NSLOTS, c.stream));
+    for (int i = 0; i < F_NSLOTS; ++i) s.f[i] = s.slab + (long long)i * vol;
+    // tables: invRc[n1] invRh[n1] invSinC[n2] invSinH[n2] cotC[n2] cotH[n2] x1c[n1] x2c[n2] x3c[n3]
+    const int n1 = c.d.n1, n2 = c.d.n2, n3 = c.d.n3;
+    size_t nt = 3 * (size_t)n1 + 4 * (size_t)n2 + (size_t)n2 + (size_t)n3;
+    std::vector<T> h(nt, T(1));
+    T* w = h.data();
+    T* invRc = w; w += n1;
+    T* invRh = w; w += n1;
+    T* invSinC = w; w += n2;
+    T* invSinH = w; w += n2;
+    T* cotC = w; w += n2;
+    T* cotH = w; w += n2;
+    T* x1c = w; w += n1;
+    T* x2c = w; w += n2;
+    T* x3c = w; w += n3;
+    for (int i = 0; i < n1; ++i) {
+        x1c[i] = T(c.hx1[i]);
+        invRc[i] = T(1.0 / c.hx1[i]);
+        if (i < n1 - 1) invRh[i] = T(1.0 / (0.5 * (c.hx1[i] + c.hx1[i + 1])));
+    }
+    for (int j = 0; j < n2; ++j) {
+        x2c[j] = T(c.hx2[j]);
+        invSinC[j] = T(1.0 / std::sin(c.hx2[j]));
+        cotC[j] = T(1.0 / std::tan(c.hx2[j]));
+        if (j < n2 - 1) {
+            double th = 0.5 * (c.hx2[j] + c.hx2[j + 1]);
+            invSinH[j] = T(1.0 / std::sin(th));
+            cotH[j] = T(1.0 / std::tan(th));
+        }
+    }
+    for (int k = 0; k < n3; ++k) x3c[k] = T(c.hx3[k]);
+    CK(cudaMalloc((void**)&s.tab, sizeof(T) * nt));
+    CK(cudaMemcpyAsync(s.tab, h.data(), sizeof(T) * nt, cudaMemcpyHostToDevice, c.stream));
+    T* t = s.tab;
+    s.geo.invRc = t; t += n1;
+    s.geo.invRh = t; t += n1;
+    s.geo.invSinC = t; t += n2;
+    s.geo.invSinH = t; t += n2;
+    s.geo.cotC = t; t += n2;
+    s.geo.cotH = t; t += n2;
+    s.geo.x1c = t; t += n1;
+    s.geo.x2c = t; t += n2;
+    s.geo.x3c = t; t += n3;
+    CK(cudaStreamSynchronize(c.stream));
+    return SPH_OK;
+}
+
+template <typename T>
+void free_state(State<T>& s) {
+    if (s.slab) cudaFree(s.slab);
+    if (s.tab) cudaFree(s.tab);
+    s.slab = nullptr; s.tab = nullptr;
+}
+
+std::vector<double> linspace(double c, double l, int n) {
+    // node coordinates spanning c - l/2 .. c + l/2 (Julia range(a, b, length=n))
+    std::vector<double> x(n);
+    const double lo = c - l / 2.0, hi = c + l / 2.0;
+    for (int i = 0; i < n; ++i) x[i] = (i == n - 1) ? hi : lo + (hi - lo) * (double)i / (double)(n - 1);
+    return x;
+}
+
+// host-side initial fields in the box layout (initialize_inclusion!, initialize_velocity!)
+int init_fields(Ctx& c) {
+    const sph_params& q = c.prm;
+    const Dims& d = c.d;
+    const long long vol = d.vol;
+    std::vector<double> rho(vol, 0.0), eta(vol, 0.0), V(vol, 0.0);
+    std::vector<uint8_t> ph(vol, 0);
+    for (int k = 0; k < d.n3; ++k)
+        for (int j = 0; j < d.n2; ++j)
+            for (int i = 0; i < d.n1; ++i) {
+                long long ci = i + (long long)d.sy * j + (long long)d.sz * k;
+                rho[ci] = q.rho0;
+                eta[ci] = q.eta0;
+                if (q.init == SPH_INIT_INCLUSION) {
+                    double x = c.hx1[i], y = c.hx2[j], z = c.hx3[k], r2;
+                    if (q.geometry == SPH_GEOM_SPHERICAL)
+                        r2 = (x - q.r) * (x - q.r) + ((y - kPi / 2.0) * q.r) * ((y - kPi / 2.0) * q.r) + (z * q.r) * (z * q.r);
+                    else if (q.geometry == SPH_GEOM_CYLINDRICAL)
+                        r2 = (x - q.r) * (x - q.r) + (y * q.r) * (y * q.r) + z * z;
+                    else
+                        r2 = x * x + y * y + z * z;
+                    if (r2 < q.radius) {
+                        rho[ci] = q.rho_in;
+                        eta[ci] = q.eta0 / q.vr;
+                        ph[ci] = q.incl_linear ? 1 : 0;
+                    }
+                }
+            }
+    State<double>& s = c.s64;
+    CK(cudaMemcpyAsync(s.f[F_RHO], rho.data(), sizeof(double) * vol, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.f[F_ETA], eta.data(), sizeof(double) * vol, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.f[F_ETA_INI], eta.data(), sizeof(double) * vol, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.f[F_ETA_PL], eta.data(), sizeof(double) * vol, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(c.phase, ph.data(), vol, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (q.init == SPH_INIT_INCLUSION) {
+        int vf = F_V3;
+        if (q.geometry == SPH_GEOM_SPHERICAL) {  // Vφ = (θ - π/2) r sh everywhere
+            for (int k = 0; k <= d.n3; ++k)
+                for (int j = 0; j < d.n2; ++j)
+                    for (int i = 0; i < d.n1; ++i) V[i + (long long)d.sy * j + (long long)d.sz * k] = (c.hx2[j] - kPi / 2.0) * q.r * q.sh;
+        } else if (q.geometry == SPH_GEOM_CYLINDRICAL) {  // VZ = θ r sh on the θ and z faces
+            for (int k = 0; k <= d.n3; ++k)
+                for (int j = 0; j < d.n2; ++j)
+                    for (int i = 0; i < d.n1; ++i)
+                        if (j == 0 || j == d.n2 - 1 || k == 0 || k == d.n3) V[i + (long long)d.sy * j + (long long)d.sz * k] = c.hx2[j] * q.r * q.sh;
+        } else {  // VX = Y sh everywhere
+            vf = F_V1;
+            for (int k = 0; k < d.n3; ++k)
+                for (int j = 0; j < d.n2; ++j)
+                    for (int i = 0; i <= d.n1; ++i) V[i + (long long)d.sy * j + (long long)d.sz * k] = c.hx2[j] * q.sh;
+        }
+        CK(cudaMemcpyAsync(s.f[vf], V.data(), sizeof(double) * vol, cudaMemcpyHostToDevice, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+    }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// precision bookkeeping: the FP64 state is the master copy for the ABI
+int sync32(Ctx& c) {
+    if (!c.has32 || !c.stale32) return SPH_OK;
+    const long long vol = c.d.vol;
+    const int slots[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23, F_ETA, F_ETA_INI, F_ETA_SM, F_DT_R, F_TII, F_RHO, F_ETA_PL};
+    for (int sl : slots) k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(c.s32.f[sl], c.s64.f[sl], vol);
+    CK(cudaGetLastError());
+    c.stale32 = false;
+    return SPH_OK;
+}
+int sync64(Ctx& c) {
+    if (!c.stale64) return SPH_OK;
+    const long long vol = c.d.vol;
+    const int slots[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23, F_ETA, F_ETA_SM, F_DT_R, F_TII, F_ETA_PL};
+    for (int sl : slots) k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(c.s64.f[sl], c.s32.f[sl], vol);
+    CK(cudaGetLastError());
+    c.stale64 = false;
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// one reference PT iteration on state s
+template <typename T, int G>
+void launch_maxloc(Ctx& c, KP<T>& p) {
+    k_maxloc<T><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p, G == CART);
+}
+
+template <typename T, int G>
+void launch_rheology(Ctx& c, State<T>& s, KP<T>& p) {
+    const int rh = c.prm.rheology;
+    const int faces_only = (G == CART);
+    if (rh == SPH_RHEO_TAU_POWER) {
+        k_rheo_tau<T, 0><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p, faces_only, T(c.cur_n));
+    } else if (rh == SPH_RHEO_TAU_POWER_RELAX) {
+        if (c.cur_n > 1.0) k_rheo_tau<T, 1><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p, faces_only, T(c.cur_n));
+    } else if (rh == SPH_RHEO_EDOT_POWER_RELAX) {
+        k_strain<T, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        k_edot_law<T, true><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        std::swap(s.f[F_ETA], s.f[F_ETA_OUT]);
+        p.eta = s.f[F_ETA]; p.eta_out = s.f[F_ETA_OUT];
+    }
+}
+
+template <typename T, int G>
+void iterate_one(Ctx& c, State<T>& s) {
+    KP<T> p = make_kp<T>(c, s);
+    launch_maxloc<T, G>(c, p);
+    k_stress<T, G, false><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+    launch_rheology<T, G>(c, s, p);
+    k_velocity<T, G, 0><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(p);
+    launch_bc<T, G>(c, p, 0);
+}
+
+template <typename T>
+void iterate_dispatch(Ctx& c, State<T>& s) {
+    switch (c.prm.geometry) {
+        case SPH_GEOM_SPHERICAL: iterate_one<T, SPH>(c, s); break;
+        case SPH_GEOM_CYLINDRICAL: iterate_one<T, CYL>(c, s); break;
+        default: iterate_one<T, CART>(c, s); break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// reductions
+template <typename T>
+void launch_maxabs(Ctx& c, const T* a, const T* b, int slot) {
+    k_maxabs<T><<<ew_blocks(c.d.vol), 256, 0, c.stream>>>(a, b, c.d.vol, c.red + slot);
+}
+inline double slot_val(Ctx& c, int i) {
+    double v;
+    std::memcpy(&v, &c.hred[i], sizeof(double));
+    return v;
+}
+int fetch_red(Ctx& c) {
+    CK(cudaMemcpyAsync(c.hred, c.red, sizeof(unsigned long long) * kRedSlots, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return SPH_OK;
+}
+
+// relative velocity change of the last iteration (the reference's err)
+template <typename T>
+int ref_err(Ctx& c, State<T>& s, double* err) {
+    CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
+    launch_maxabs<T>(c, s.f[F_V1], s.f[F_V1E], 0);
+    launch_maxabs<T>(c, s.f[F_V2], s.f[F_V2E], 1);
+    launch_maxabs<T>(c, s.f[F_V3], s.f[F_V3E], 2);
+    launch_maxabs<T>(c, s.f[F_V1], nullptr, 3);
+    launch_maxabs<T>(c, s.f[F_V2], nullptr, 4);
+    launch_maxabs<T>(c, s.f[F_V3], nullptr, 5);
+    CK(cudaGetLastError());
+    int rc = fetch_red(c);
+    if (rc) return rc;
+    double e = 0.0;
+    for (int f = 0; f < 3; ++f) {
+        double dv = slot_val(c, f), vv = slot_val(c, 3 + f);
+        double r = dv / vv;
+        if (!(r == r)) { e = r; break; }
+        e = std::max(e, r);
+    }
+    *err = e;
+    return SPH_OK;
+}
+
+template <typename T>
+int snapshot(Ctx& c, State<T>& s) {
+    const size_t b = sizeof(T) * c.d.vol;
+    CK(cudaMemcpyAsync(s.f[F_V1E], s.f[F_V1], b, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.f[F_V2E], s.f[F_V2], b, cudaMemcpyDeviceToDevice, c.stream));
+    CK(cudaMemcpyAsync(s.f[F_V3E], s.f[F_V3], b, cudaMemcpyDeviceToDevice, c.stream));
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 residual of the FP64 state (see sph_residual in sphstokes.h)
+template <int G>
+int residual64_g(Ctx& c, double out[7], bool eta_from_law) {
+    State<double>& s = c.s64;
+    KP<double> p = make_kp<double>(c, s);
+    const double* eta_eff = s.f[F_ETA];
+    if (eta_from_law) {
+        k_strain<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        k_edot_law<double, false><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        eta_eff = s.f[F_ETA_OUT];
+    }
+    KP<double> r = p;
+    r.eta = const_cast<double*>(eta_eff);
+    r.t11 = s.f[F_Q11]; r.t22 = s.f[F_Q22]; r.t33 = s.f[F_Q33]; r.t12 = s.f[F_Q12]; r.t13 = s.f[F_Q13]; r.t23 = s.f[F_Q23];
+    k_tau_visc<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(r);
+    k_velocity<double, G, 2><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(r);
+    CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
+    launch_maxabs<double>(c, s.f[F_RV1], nullptr, 0);
+    launch_maxabs<double>(c, s.f[F_RV2], nullptr, 1);
+    launch_maxabs<double>(c, s.f[F_RV3], nullptr, 2);
+    launch_maxabs<double>(c, s.f[F_RP], nullptr, 3);
+    launch_maxabs<double>(c, s.f[F_V1], nullptr, 4);
+    launch_maxabs<double>(c, s.f[F_V2], nullptr, 5);
+    launch_maxabs<double>(c, s.f[F_V3], nullptr, 6);
+    CK(cudaGetLastError());
+    int rc = fetch_red(c);
+    if (rc) return rc;
+    for (int i = 0; i < 4; ++i) out[i] = slot_val(c, i);
+    out[4] = std::max(slot_val(c, 4), std::max(slot_val(c, 5), slot_val(c, 6)));
+    out[5] = c.f_scale;
+    const double mom = std::max(out[0], std::max(out[1], out[2])) / c.f_scale;
+    const double vs = out[4] > 0.0 ? out[4] : 1.0;
+    const double cont = out[3] * c.prm.l1 / vs;
+    out[6] = (mom != mom || cont != cont) ? NAN : std::max(mom, cont);
+    return SPH_OK;
+}
+
+int residual64(Ctx& c, double out[7]) {
+    const bool law = c.prm.rheology == SPH_RHEO_EDOT_POWER_RELAX;
+    switch (c.prm.geometry) {
+        case SPH_GEOM_SPHERICAL: return residual64_g<SPH>(c, out, law);
+        case SPH_GEOM_CYLINDRICAL: return residual64_g<CYL>(c, out, law);
+        default: return residual64_g<CART>(c, out, law);
+    }
+}
+
+int compute_f_scale(Ctx& c) {
+    CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
+    launch_maxabs<double>(c, c.s64.f[F_RHO], nullptr, 0);
+    int rc = fetch_red(c);
+    if (rc) return rc;
+    const sph_params& q = c.prm;
+    double f = slot_val(c, 0) * std::fabs(q.g);
+    if (q.bc == SPH_BC_STRESS) f = std::max(f, std::max(std::fabs(q.sig_bc[1]), std::fabs(q.sig_bc[2])) / q.l1);
+    c.f_scale = f > 0.0 ? f : 1.0;
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// plain PT solve (FP64 or FP32 state)
+template <typename T>
+int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_solve_info* info, int64_t* hi, double* he, int64_t cap) {
+    const int nout = o.nout > 0 ? o.nout : 100;
+    int64_t it = 0;
+    double err = 1.0;
+    int status = SPH_ERR_NOT_CONVERGED;
+    while (it < o.maxiter) {
+        ++it;
+        const bool check = (it % nout) == 0;
+        if (check && o.criterion == SPH_CRIT_REFERENCE) {
+            int rc = snapshot<T>(c, s);
+            if (rc) return rc;
+        }
+        iterate_dispatch<T>(c, s);
+        if (!check) continue;
+        CK(cudaGetLastError());
+        if (o.criterion == SPH_CRIT_REFERENCE) {
+            int rc = ref_err<T>(c, s, &err);
+            if (rc) return rc;
+        } else {
+            if (is32) { c.stale64 = true; int rc = sync64(c); if (rc) return rc; }
+            double out[7];
+            int rc = residual64(c, out);
+            if (rc) return rc;
+            err = out[6];
+        }
+        if (info && info->nhist < cap) {
+            if (hi) hi[info->nhist] = it;
+            if (he) he[info->nhist] = err;
+            info->nhist++;
+        }
+        if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
+        if (c.prm.switch_err > 0.0 && err < c.prm.switch_err) c.cur_n = c.prm.n_exp_late;
+        if (err < o.tol && (o.criterion != SPH_CRIT_REFERENCE || it > 20)) { status = SPH_OK; break; }
+    }
+    if (info) { info->iters = it; info->err = err; info->status = status; }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision: FP32 PT sweeps on the correction problem inside an FP64
+// defect-correction loop.
+//   r_V = momentum residual of (V, P) with η = η_eff(V) (FP64), r_P = div V (FP64)
+//   inner: PT on (δV, δP, δτ) with η frozen at η_eff, homogeneous BCs,
+//          δP -= KBDT (div δV + r_P), δV += DT_R (div(-δP + δτ) + r_V)
+//   V += δV, P += δP (FP64)
+template <int G>
+int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t* hi, double* he, int64_t cap) {
+    State<double>& s = c.s64;
+    State<float>& t = c.s32;
+    const long long vol = c.d.vol;
+    const int nout = o.nout > 0 ? o.nout : 100;
+    const bool law = c.prm.rheology == SPH_RHEO_EDOT_POWER_RELAX;
+    if (c.prm.rheology == SPH_RHEO_TAU_POWER || c.prm.rheology == SPH_RHEO_TAU_POWER_RELAX)
+        return fail(SPH_ERR_UNSUPPORTED, "mixed precision needs an explicit viscosity law (linear or strain-rate power law)");
+    int64_t iters = 0;
+    int status = SPH_ERR_NOT_CONVERGED;
+    double err = 1.0;
+    // optional FP32 nonlinear warm start on the full variables
+    if (o.warm_tol > 0.0) {
+        int rc = sync32(c);
+        if (rc) return rc;
+        double werr = 1.0;
+        while (iters < o.maxiter) {
+            ++iters;
+            const bool check = (iters % nout) == 0;
+            if (check) { rc = snapshot<float>(c, t); if (rc) return rc; }
+            iterate_dispatch<float>(c, t);
+            if (!check) continue;
+            rc = ref_err<float>(c, t, &werr);
+            if (rc) return rc;
+            if (!(werr == werr)) return fail(SPH_ERR_DIVERGED, "NaN in the FP32 warm start");
+            if (werr < o.warm_tol && iters > 20) break;
+        }
+        // widen V, P (η is recomputed from the law)
+        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
+        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
+        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
+        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
+        if (!law) k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_ETA], t.f[F_ETA], vol);
+        CK(cudaGetLastError());
+    }
+    KP<double> p = make_kp<double>(c, s);
+    for (int outer = 0; outer <= o.max_outer; ++outer) {
+        // η_eff(V) in FP64, then the full BC program (stress ghosts use η_eff)
+        if (law) {
+            k_strain<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+            k_edot_law<double, false><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+            CK(cudaMemcpyAsync(s.f[F_ETA], s.f[F_ETA_OUT], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
+        }
+        launch_bc<double, G>(c, p, 0);
+        double out[7];
+        int rc = residual64_g<G>(c, out, false);
+        if (rc) return rc;
+        err = out[6];
+        if (info) {
+            if (info->nhist < cap) {
+                if (hi) hi[info->nhist] = iters;
+                if (he) he[info->nhist] = err;
+                info->nhist++;
+            }
+            info->outer = outer;
+            info->residual = err;
+        }
+        if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
+        if (err < o.tol) { status = SPH_OK; break; }
+        if (outer == o.max_outer || iters >= o.maxiter) break;
+        // frozen coefficients and right-hand sides of the correction problem
+        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_ETA], s.f[F_ETA], vol);
+        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV1], s.f[F_RV1], vol);
+        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV2], s.f[F_RV2], vol);
+        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV3], s.f[F_RV3], vol);
+        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RP], s.f[F_RP], vol);
+        const int zero[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
+        for (int z : zero) CK(cudaMemsetAsync(t.f[z], 0, sizeof(float) * vol, c.stream));
+        KP<float> q = make_kp<float>(c, t);
+        launch_maxloc<float, G>(c, q);
+        const double r0 = std::max(out[0], std::max(out[1], out[2]));
+        const int inner_max = o.inner_max > 0 ? o.inner_max : 100000;
+        int inner = 0;
+        while (inner < inner_max && iters < o.maxiter) {
+            ++inner; ++iters;
+            k_stress<float, G, true><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(q);
+            k_velocity<float, G, 1><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
+            launch_bc<float, G>(c, q, 1);
+            if (inner % nout) continue;
+            // momentum residual of the correction problem with the current δ state
+            CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
+            k_velocity_norm<float, G><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
+            CK(cudaGetLastError());
+            rc = fetch_red(c);
+            if (rc) return rc;
+            const double ri = slot_val(c, 0);
+            if (!(ri == ri)) return fail(SPH_ERR_DIVERGED, "NaN in the FP32 correction sweeps");
+            if (ri <= o.inner_rtol * r0) break;
+        }
+        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
+        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
+        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
+        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
+        CK(cudaGetLastError());
+    }
+    // final τ = 2 η_eff D(V) of the FP64 state as the stress output
+    {
+        const int q[6] = {F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23};
+        const int d[6] = {F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
+        for (int i = 0; i < 6; ++i) CK(cudaMemcpyAsync(s.f[d[i]], s.f[q[i]], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    c.stale32 = true;
+    c.stale64 = false;
+    if (info) { info->iters = iters; info->err = err; info->status = status; }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
+int check_params(const sph_params* p) {
+    if (!p) return fail(SPH_ERR_INVALID, "params is NULL");
+    if (p->abi_version != SPH_ABI_VERSION) return fail(SPH_ERR_INVALID, "abi_version mismatch");
+    if (p->geometry < 0 || p->geometry > 2) return fail(SPH_ERR_INVALID, "geometry");
+    if (p->precision < 0 || p->precision > 2) return fail(SPH_ERR_INVALID, "precision");
+    if (p->rheology < 0 || p->rheology > 3) return fail(SPH_ERR_INVALID, "rheology");
+    if (p->bc < 0 || p->bc > 2) return fail(SPH_ERR_INVALID, "bc");
+    if (p->n1 < 5 || p->n2 < 5 || p->n3 < 5) return fail(SPH_ERR_INVALID, "grid needs at least 5 cells per axis");
+    if (!(p->l1 > 0 && p->l2 > 0 && p->l3 > 0 && p->l_ref > 0)) return fail(SPH_ERR_INVALID, "lengths must be positive");
+    long long px = ((p->n1 + 1 + 31) / 32) * 32LL;
+    if (px * (p->n2 + 1LL) * (p->n3 + 1LL) >= (1LL << 31)) return fail(SPH_ERR_INVALID, "grid too large for 32-bit indexing");
+    if (p->geometry == SPH_GEOM_SPHERICAL) {
+        if (p->c1 - p->l1 / 2 <= 0) return fail(SPH_ERR_INVALID, "spherical radius range must be positive");
+        if (p->c2 - p->l2 / 2 <= 0 || p->c2 + p->l2 / 2 >= kPi) return fail(SPH_ERR_INVALID, "colatitude range must be inside (0, pi)");
+    }
+    if (p->geometry == SPH_GEOM_CYLINDRICAL && p->c1 - p->l1 / 2 <= 0) return fail(SPH_ERR_INVALID, "cylindrical radius range must be positive");
+    return SPH_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+int sph_abi_version(void) { return SPH_ABI_VERSION; }
+
+const char* sph_last_error(void) { return g_err.c_str(); }
+
+const char* sph_strerror(int code) {
+    switch (code) {
+        case SPH_OK: return "ok";
+        case SPH_ERR_INVALID: return "invalid argument";
+        case SPH_ERR_CUDA: return "CUDA error";
+        case SPH_ERR_NOT_CONVERGED: return "not converged";
+        case SPH_ERR_DIVERGED: return "diverged (NaN/Inf)";
+        case SPH_ERR_NOMEM: return "out of memory";
+        case SPH_ERR_UNSUPPORTED: return "unsupported option combination";
+        case SPH_ERR_NO_DEVICE: return "no usable CUDA device";
+        default: return "unknown status";
+    }
+}
+
+int sph_params_default(sph_params* p, int32_t geometry) {
+    if (!p) return fail(SPH_ERR_INVALID, "params is NULL");
+    std::memset(p, 0, sizeof(*p));
+    p->abi_version = SPH_ABI_VERSION;
+    p->geometry = geometry;
+    p->precision = SPH_PREC_FP64;
+    p->bc = SPH_BC_DIAPIR;
+    p->init = SPH_INIT_INCLUSION;
+    p->n1 = p->n2 = p->n3 = 208 - 1;
+    p->eta0 = 1.0; p->vr = 1e2; p->rho0 = 0.0; p->rho_in = -10.0; p->g = 1.0;
+    p->tau_C = 1.0; p->radius = 1.0; p->sh = 1.0; p->dmp = 4.5;
+    p->relax = 1e-3; p->edot_bg = 1.0;
+    const double lr = 6.0;
+    switch (geometry) {
+        case SPH_GEOM_SPHERICAL:  // SphericalStokes_diapir.jl:348-367
+            p->rheology = SPH_RHEO_TAU_POWER; p->n_exp = 5.0; p->r = 1000.0;
+            p->c1 = p->r; p->c2 = kPi / 2.0; p->c3 = 0.0;
+            p->l1 = lr; p->l2 = lr / p->r; p->l3 = lr / p->r; p->l_ref = lr;
+            break;
+        case SPH_GEOM_CYLINDRICAL:  // CylindricalStokes_diapir.jl:227-251
+            p->rheology = SPH_RHEO_TAU_POWER_RELAX; p->n_exp = 1.0; p->n_exp_late = 5.0; p->switch_err = 1e-5; p->r = 1000.0;
+            p->c1 = p->r; p->c2 = 0.0; p->c3 = 0.0;
+            p->l1 = lr; p->l2 = lr / p->r; p->l3 = lr; p->l_ref = lr;
+            break;
+        case SPH_GEOM_CARTESIAN:  // CartesianStokes_diapir.jl:267-289
+            p->rheology = SPH_RHEO_TAU_POWER_RELAX; p->n_exp = 5.0; p->r = 0.0;
+            p->c1 = p->c2 = p->c3 = 0.0;
+            p->l1 = p->l2 = p->l3 = lr; p->l_ref = lr;
+            break;
+        default: return fail(SPH_ERR_INVALID, "geometry");
+    }
+    p->vpdt = 0.0;  // 0: dx1 * CFL with CFL = 1/(2 + 4.5 log10(vr)), set at sph_create
+    return SPH_OK;
+}
+
+int sph_field_dims(const sph_params* p, int32_t field, int64_t dims[3]) {
+    if (!p || !dims) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (field < 0 || field >= SPH_FIELD_COUNT) return fail(SPH_ERR_INVALID, "field");
+    Dims d{}; d.n1 = p->n1; d.n2 = p->n2; d.n3 = p->n3;
+    int e[3];
+    field_extent(d, field, e);
+    dims[0] = e[0]; dims[1] = e[1]; dims[2] = e[2];
+    return SPH_OK;
+}
+
+int sph_create(const sph_params* prm, void** out) {
+    if (!out) return fail(SPH_ERR_INVALID, "ctx out pointer is NULL");
+    *out = nullptr;
+    int rc = check_params(prm);
+    if (rc) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(SPH_ERR_NO_DEVICE, "no CUDA device");
+    Ctx* c = new (std::nothrow) Ctx();
+    if (!c) return fail(SPH_ERR_NOMEM, "host allocation");
+    c->prm = *prm;
+    sph_params& q = c->prm;
+    if (q.vpdt <= 0.0) q.vpdt = q.l1 / (q.n1 - 1) * (1.0 / (2.0 + 4.5 * std::log10(q.vr)));
+    c->cur_n = q.n_exp;
+    Dims& d = c->d;
+    d.n1 = q.n1; d.n2 = q.n2; d.n3 = q.n3;
+    d.px = ((q.n1 + 1 + 31) / 32) * 32; d.py = q.n2 + 1; d.pz = q.n3 + 1;
+    d.sy = d.px; d.sz = d.px * d.py;
+    d.vol = (long long)d.px * d.py * d.pz;
+    c->hx1 = linspace(q.c1, q.l1, q.n1);
+    c->hx2 = linspace(q.c2, q.l2, q.n2);
+    c->hx3 = linspace(q.c3, q.l3, q.n3);
+    auto cleanup = [&](int code) { sph_destroy(c); return code; };
+    if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(fail(SPH_ERR_CUDA, "stream create"));
+    c->stream = c->own_stream;
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return cleanup(fail(SPH_ERR_CUDA, "event create"));
+    if (cudaMalloc((void**)&c->red, sizeof(unsigned long long) * kRedSlots) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "reduction slots"));
+    if (cudaMallocHost((void**)&c->hred, sizeof(unsigned long long) * kRedSlots) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "pinned slots"));
+    if (cudaMalloc((void**)&c->phase, d.vol) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "phase"));
+    if ((rc = alloc_state<double>(*c, c->s64))) return cleanup(rc == SPH_ERR_CUDA ? SPH_ERR_NOMEM : rc);
+    if (q.precision != SPH_PREC_FP64) {
+        if ((rc = alloc_state<float>(*c, c->s32))) return cleanup(rc == SPH_ERR_CUDA ? SPH_ERR_NOMEM : rc);
+        c->has32 = true;
+    }
+    if ((rc = build_bc(*c))) return cleanup(rc);
+    if ((rc = init_fields(*c))) return cleanup(rc);
+    if ((rc = compute_f_scale(*c))) return cleanup(rc);
+    c->stale32 = true;
+    *out = c;
+    return SPH_OK;
+}
+
+int sph_destroy(void* h) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return SPH_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_state(c->s64);
+    free_state(c->s32);
+    if (c->phase) cudaFree(c->phase);
+    if (c->red) cudaFree(c->red);
+    if (c->hred) cudaFreeHost(c->hred);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
+    delete c;
+    return SPH_OK;
+}
+
+int sph_set_stream(void* h, void* stream) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    CK(cudaStreamSynchronize(c->stream));
+    c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
+    return SPH_OK;
+}
+
+static int copy_field(Ctx* c, int32_t field, double* host, const double* src_host, int64_t count) {
+    if (field < 0 || field >= SPH_FIELD_COUNT) return fail(SPH_ERR_INVALID, "field");
+    int e[3];
+    field_extent(c->d, field, e);
+    const int64_t need = (int64_t)e[0] * e[1] * e[2];
+    if (count != need) return fail(SPH_ERR_INVALID, "count does not match the field size");
+    if (!host && !src_host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    const bool get = host != nullptr;
+    if (get) { int rc = sync64(*c); if (rc) return rc; }
+    if (field == SPH_FIELD_PHASE) {
+        std::vector<uint8_t> b((size_t)c->d.vol, 0);
+        if (get) { CK(cudaMemcpyAsync(b.data(), c->phase, c->d.vol, cudaMemcpyDeviceToHost, c->stream)); CK(cudaStreamSynchronize(c->stream)); }
+        for (int k = 0; k < e[2]; ++k)
+            for (int j = 0; j < e[1]; ++j)
+                for (int i = 0; i < e[0]; ++i) {
+                    long long bi = i + (long long)c->d.sy * j + (long long)c->d.sz * k;
+                    long long hi = i + (long long)e[0] * (j + (long long)e[1] * k);
+                    if (get) host[hi] = b[bi]; else b[bi] = src_host[hi] != 0.0 ? 1 : 0;
+                }
+        if (!get) { CK(cudaMemcpyAsync(c->phase, b.data(), c->d.vol, cudaMemcpyHostToDevice, c->stream)); CK(cudaStreamSynchronize(c->stream)); c->stale32 = true; }
+        return SPH_OK;
+    }
+    double* dev = c->s64.f[slot_of(field)];
+    cudaMemcpy3DParms m;
+    std::memset(&m, 0, sizeof(m));
+    cudaPitchedPtr dp = make_cudaPitchedPtr(dev, sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
+    cudaPitchedPtr hp = make_cudaPitchedPtr(get ? (void*)host : (void*)src_host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
+    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
+    if (get) { m.srcPtr = dp; m.dstPtr = hp; m.kind = cudaMemcpyDeviceToHost; }
+    else { m.srcPtr = hp; m.dstPtr = dp; m.kind = cudaMemcpyHostToDevice; }
+    CK(cudaMemcpy3DAsync(&m, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (!get) c->stale32 = true;
+    return SPH_OK;
+}
+
+int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    int rc = sync64(*c);
+    if (rc) return rc;
+    rc = copy_field(c, field, nullptr, host, count);
+    if (rc) return rc;
+    if (field == SPH_FIELD_RHO) return compute_f_scale(*c);
+    return SPH_OK;
+}
+
+int sph_get_field(void* h, int32_t field, double* host, int64_t count) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    return copy_field(c, field, host, nullptr, count);
+}
+
+int sph_step(void* h, int64_t k) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
+    const bool use32 = c->prm.precision != SPH_PREC_FP64;
+    int rc = use32 ? sync32(*c) : sync64(*c);
+    if (rc) return rc;
+    CK(cudaEventRecord(c->ev0, c->stream));
+    for (int64_t i = 0; i < k; ++i) {
+        if (use32) iterate_dispatch<float>(*c, c->s32);
+        else iterate_dispatch<double>(*c, c->s64);
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    if (use32) c->stale64 = true;
+    return SPH_OK;
+}
+
+int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* hist_iter, double* hist_err, int64_t hist_cap) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !o) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (o->tol <= 0.0 || o->maxiter <= 0) return fail(SPH_ERR_INVALID, "tol and maxiter must be positive");
+    sph_solve_info local;
+    std::memset(&local, 0, sizeof(local));
+    sph_solve_info* inf = info ? info : &local;
+    std::memset(inf, 0, sizeof(*inf));
+    auto t0 = std::chrono::steady_clock::now();
+    CK(cudaEventRecord(c->ev0, c->stream));
+    int rc;
+    const int prec = c->prm.precision;
+    if (prec == SPH_PREC_MIXED) {
+        if (o->criterion != SPH_CRIT_RESIDUAL) return fail(SPH_ERR_UNSUPPORTED, "mixed precision stops on the FP64 residual (SPH_CRIT_RESIDUAL)");
+        rc = sync64(*c);
+        if (rc) return rc;
+        switch (c->prm.geometry) {
+            case SPH_GEOM_SPHERICAL: rc = solve_mixed_g<SPH>(*c, *o, inf, hist_iter, hist_err, hist_cap); break;
+            case SPH_GEOM_CYLINDRICAL: rc = solve_mixed_g<CYL>(*c, *o, inf, hist_iter, hist_err, hist_cap); break;
+            default: rc = solve_mixed_g<CART>(*c, *o, inf, hist_iter, hist_err, hist_cap); break;
+        }
+    } else if (prec == SPH_PREC_FP32) {
+        rc = sync32(*c);
+        if (!rc) rc = solve_plain<float>(*c, c->s32, true, *o, inf, hist_iter, hist_err, hist_cap);
+        c->stale64 = true;
+    } else {
+        rc = sync64(*c);
+        if (!rc) rc = solve_plain<double>(*c, c->s64, false, *o, inf, hist_iter, hist_err, hist_cap);
+        c->stale32 = true;
+    }
+    if (rc) return rc;
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    inf->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    {
+        rc = sync64(*c);
+        if (rc) return rc;
+        double out[7];
+        rc = residual64(*c, out);
+        if (rc) return rc;
+        inf->residual = out[6];
+    }
+    return inf->status;
+}
+
+int sph_residual(void* h, double out[7]) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !out) return fail(SPH_ERR_INVALID, "NULL argument");
+    int rc = sync64(*c);
+    if (rc) return rc;
+    return residual64(*c, out);
+}
+
+int sph_run_kernel(void* h, int32_t kernel) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (c->prm.precision != SPH_PREC_FP64) return fail(SPH_ERR_UNSUPPORTED, "single kernels run on the FP64 state");
+    int rc = sync64(*c);
+    if (rc) return rc;
+    State<double>& s = c->s64;
+    KP<double> p = make_kp<double>(*c, s);
+    const int G = c->prm.geometry;
+    switch (kernel) {
+        case SPH_K_MAXLOC:
+            if (G == SPH) launch_maxloc<double, SPH>(*c, p); else if (G == CYL) launch_maxloc<double, CYL>(*c, p); else launch_maxloc<double, CART>(*c, p);
+            break;
+        case SPH_K_COMPUTE_P:
+            if (G == SPH) k_stress<double, SPH, false><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+            else if (G == CYL) k_stress<double, CYL, false><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+            else k_stress<double, CART, false><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+            break;
+        case SPH_K_RHEOLOGY:
+            if (G == SPH) launch_rheology<double, SPH>(*c, s, p); else if (G == CYL) launch_rheology<double, CYL>(*c, s, p); else launch_rheology<double, CART>(*c, s, p);
+            break;
+        case SPH_K_COMPUTE_V:
+            if (G == SPH) k_velocity<double, SPH, 0><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p);
+            else if (G == CYL) k_velocity<double, CYL, 0><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p);
+            else k_velocity<double, CART, 0><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p);
+            break;
+        case SPH_K_BC:
+            if (G == SPH) launch_bc<double, SPH>(*c, p, 0); else if (G == CYL) launch_bc<double, CYL>(*c, p, 0); else launch_bc<double, CART>(*c, p, 0);
+            break;
+        default: return fail(SPH_ERR_INVALID, "kernel id");
+    }
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_last_device_ms(void* h, double* ms) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !ms) return fail(SPH_ERR_INVALID, "NULL argument");
+    *ms = c->last_ms;
+    return SPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,143 @@
+"""GPU parity: the CUDA kernels (through the C ABI) against the FP64 oracle.
+
+Tolerances are relative to each field's max-norm: 1e-12 for single kernels,
+1e-9 for fixed-iteration trajectories (FMA contraction and the algebraic form
+e/(e+GSDT) of 1/(1+GSDT/e) differ from the oracle at the last bits only).
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import sphericalstokes_gb300 as S
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("P", "V1", "V2", "V3", "TAU11", "TAU22", "TAU33", "TAU12", "TAU13", "TAU23", "ETA", "ETA_SM", "DT_R", "TII")
+
+
+def relerr(a, b):
+    scale = max(np.abs(b).max(), 1e-300)
+    return float(np.abs(a - b).max() / scale)
+
+
+def randomize(o, sv, rng, fields=FIELDS + ("RHO", "ETA_INI")):
+    for f in fields:
+        a = o.field(f)
+        if f.startswith("ETA") or f == "DT_R":
+            a[:] = np.exp(rng.uniform(-2, 2, a.shape))
+        elif f == "TII":
+            a[:] = rng.uniform(0.1, 2.0, a.shape)
+        else:
+            a[:] = rng.standard_normal(a.shape)
+        sv.set(f, a)
+
+
+def compare(o, sv, fields, tol):
+    bad = {}
+    for f in fields:
+        e = relerr(sv.get(f), o.field(f))
+        if not e < tol:
+            bad[f] = e
+    assert not bad, bad
+
+
+GRIDS = [(13, 9, 11), (8, 16, 7)]
+
+
+@pytest.mark.parametrize("n", GRIDS)
+@pytest.mark.parametrize("bc", ["diapir", "free_slip", "stress"])
+def test_single_kernels_spherical(n, bc):
+    p = S.default_params("spherical", n1=n[0], n2=n[1], n3=n[2], bc=bc, n_exp=3.0, sig_bc=(0.0, 0.5, -0.5))
+    rng = np.random.default_rng(1)
+    with S.Solver(p) as sv:
+        o = oracle.Sph.from_params(p)
+        randomize(o, sv, rng)
+        sv.maxloc(); o.maxloc()
+        compare(o, sv, ["ETA_SM"], 1e-15)
+        randomize(o, sv, rng)
+        sv.compute_P(); o.compute_P()
+        compare(o, sv, ["P", "TAU11", "TAU22", "TAU33", "TAU12", "TAU13", "TAU23", "DT_R"], 1e-12)
+        sv.power_law(); o.power_law()
+        compare(o, sv, ["TII", "ETA"], 1e-12)
+        sv.compute_V(); o.compute_V()
+        compare(o, sv, ["V1", "V2", "V3"], 1e-12)
+        sv.apply_bc(); o.apply_bc()
+        compare(o, sv, ["V1", "V2", "V3"], 1e-12)
+
+
+@pytest.mark.parametrize("k", [1, 10, 100])
+def test_trajectory_spherical_diapir(k):
+    # SphericalStokes_diapir.jl setup (n_exp = 5, r = 1000, lr = 6) on a small grid
+    p = S.default_params("spherical", n1=17, n2=15, n3=13)
+    with S.Solver(p) as sv:
+        sv.step(k)
+        o = oracle.Sph.from_params(p)
+        o.iterate(k)
+        compare(o, sv, FIELDS, 1e-9)
+
+
+@pytest.mark.parametrize("k", [1, 50])
+def test_trajectory_free_slip_plateau_bcs(k):
+    p = S.sector_params((15, 13, 11), bc="free_slip", rheology="linear")
+    with S.Solver(p) as sv:
+        sv.step(k)
+        o = oracle.Sph.from_params(p)
+        o.iterate(k)
+        compare(o, sv, ("P", "V1", "V2", "V3", "TAU11", "TAU12", "TAU13", "TAU23", "DT_R"), 1e-9)
+
+
+@pytest.mark.parametrize("k", [1, 50])
+def test_trajectory_stress_bc_strain_rate_law(k):
+    p = S.sector_params((15, 13, 11), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5,
+                        edot_bg=0.25, sig_bc=(0.0, 0.5, -0.5), incl_linear=1)
+    with S.Solver(p) as sv:
+        sv.step(k)
+        o = oracle.Sph.from_params(p)
+        o.iterate(k)
+        compare(o, sv, ("P", "V1", "V2", "V3", "TAU11", "TAU22", "TAU12", "TAU23", "ETA"), 1e-9)
+
+
+def test_residual_matches_oracle():
+    p = S.sector_params((15, 13, 11), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5,
+                        edot_bg=0.25, sig_bc=(0.0, 0.5, -0.5), incl_linear=1)
+    with S.Solver(p) as sv:
+        sv.step(30)
+        r = sv.residual()
+        o = oracle.Sph.from_params(p)
+        o.iterate(30)
+        ro = o.residual(f_scale=r["f_scale"])
+    for key in ("mom1", "mom2", "mom3", "div", "vmax"):
+        assert abs(r[key] - ro[key]) <= 1e-9 * max(abs(ro[key]), 1e-300), (key, r[key], ro[key])
+
+
+def test_fp32_follows_fp64():
+    p = S.sector_params((15, 13, 11), bc="free_slip", rheology="linear")
+    with S.Solver(p) as a:
+        a.step(50)
+        ref = {f: a.get(f) for f in ("V1", "V2", "V3", "P")}
+    set_p = S.sector_params((15, 13, 11), bc="free_slip", rheology="linear", precision="fp32")
+    with S.Solver(set_p) as b:
+        b.step(50)
+        for f, r in ref.items():
+            assert relerr(b.get(f), r) < 1e-4, f
+
+
+def test_reference_criterion_solve_small():
+    p = S.default_params("spherical", n1=15, n2=13, n3=11)
+    with S.Solver(p) as sv:
+        res = sv.solve(tol=5e-7, maxiter=20000, nout=100, criterion="reference")
+    o = oracle.Sph.from_params(p)
+    # replay the oracle for the same number of iterations and the same err sequence
+    errs = []
+    for it in range(1, res.iters + 1):
+        if it % 100 == 0:
+            o.equal3()
+        o.iterate(1)
+        if it % 100 == 0:
+            errs.append(o.check_err())
+    assert res.converged
+    assert len(errs) == len(res.hist_err)
+    np.testing.assert_allclose(res.hist_err, errs, rtol=1e-6)
+    assert errs[-1] < 5e-7 and all(e >= 5e-7 for e in errs[:-1])

@@ -140,6 +140,22 @@ class Sph:
         o.eta_ini[:] = o.eta
         return o
 
+    @classmethod
+    def from_golden(cls, g, bc: int) -> "Sph":
+        """Oracle state from a golden file of a spherical script: its coordinates, scalars and initial fields."""
+        sc = eval(str(g["scalars_json"]))
+        x1, x2, x3 = g["coord_R_i"], g["coord_θ_i"], g["coord_φ_i"]
+        nr, nt, np_ = len(x1), len(x2), len(x3)
+        o = cls(nr, nt, np_, r=sc["r"], c1=0.5 * (x1[0] + x1[-1]), c2=0.5 * (x2[0] + x2[-1]), c3=0.5 * (x3[0] + x3[-1]),
+                lr=sc["lr"], lt=sc["lθ"], lp=sc["lφ"], l_ref=sc["lr"], dmp=sc["dmp"], vpdt=sc["vpdt"], g=sc["g"],
+                tau_C=sc["τ_C"], n_exp=sc["n_exp"], sh=sc.get("sh", 0.0), bc=bc, rheo=0)
+        o.R[:] = x1[:, None, None]
+        o.th[:] = x2[None, :, None]
+        o.ph[:] = x3[None, None, :]
+        for jn, canon in SCRIPT_NAMES["spherical"].items():
+            o.field(canon)[:] = g["in_" + jn]
+        return o
+
     def field(self, name: str) -> np.ndarray:
         return getattr(self, self.NAMES[name])
 
@@ -196,3 +212,77 @@ def set_threads(n: int):
 
 def num_threads() -> int:
     return int(lib().orc_num_threads())
+
+
+# ---------------------------------------------------------------------------
+# cylindrical / Cartesian scripts (oracle_cyl_cart.cpp)
+class CCState(C.Structure):
+    _fields_ = [("n1", C.c_int64), ("n2", C.c_int64), ("n3", C.c_int64)] + [
+        (n, _PD) for n in ("P", "V1", "V2", "V3", "t11", "t22", "t33", "t12", "t13", "t23", "rho", "eta", "eta_ini",
+                           "eta_pl", "etaSM", "DT_R", "tII", "x1", "x2", "x3")]
+
+
+class CCParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("d1", "d2", "d3", "dmp", "vpdt", "lr", "g", "tau_C", "n_exp", "relax", "r", "sh")]
+
+
+# reference array names of each script -> canonical field names
+SCRIPT_NAMES = {
+    "spherical": {"P": "P", "VR": "V1", "Vθ": "V2", "Vφ": "V3", "τ_RR": "TAU11", "τ_θθ": "TAU22", "τ_φφ": "TAU33",
+                  "τ_Rθ": "TAU12", "τ_Rφ": "TAU13", "τ_θφ": "TAU23", "η": "ETA", "η_ini": "ETA_INI", "ηSM": "ETA_SM",
+                  "DT_R": "DT_R", "τII": "TII", "ρ": "RHO"},
+    "cylindrical": {"P": "P", "VR": "V1", "Vθ": "V2", "VZ": "V3", "τ_RR": "TAU11", "τ_θθ": "TAU22", "τ_ZZ": "TAU33",
+                    "τ_Rθ": "TAU12", "τ_RZ": "TAU13", "τ_θZ": "TAU23", "η": "ETA", "η_INI": "ETA_INI", "ηSM": "ETA_SM",
+                    "DT_R": "DT_R", "τII": "TII", "ρ": "RHO", "η_PL": "ETA_PL"},
+    "cartesian": {"P": "P", "VX": "V1", "VY": "V2", "VZ": "V3", "τ_XX": "TAU11", "τ_YY": "TAU22", "τ_ZZ": "TAU33",
+                  "τ_XY": "TAU12", "τ_XZ": "TAU13", "τ_YZ": "TAU23", "η": "ETA", "η_INI": "ETA_INI", "ηSM": "ETA_SM",
+                  "DT_R": "DT_R", "τII": "TII", "ρ": "RHO", "η_PL": "ETA_PL"},
+}
+_CC_ATTR = {"P": "P", "V1": "V1", "V2": "V2", "V3": "V3", "TAU11": "t11", "TAU22": "t22", "TAU33": "t33", "TAU12": "t12",
+            "TAU13": "t13", "TAU23": "t23", "RHO": "rho", "ETA": "eta", "ETA_INI": "eta_ini", "ETA_PL": "eta_pl",
+            "ETA_SM": "etaSM", "DT_R": "DT_R", "TII": "tII"}
+
+
+class CC:
+    """State of one cylindrical or Cartesian diapir solve (numpy arrays, reference layout)."""
+
+    def __init__(self, geometry: str, fields: dict, x1, x2, x3, *, d1, d2, d3, dmp, vpdt, lr, g, tau_C, n_exp, relax, r, sh):
+        self.geometry = geometry
+        self.arr = {k: np.asfortranarray(np.array(v, dtype=np.float64)) for k, v in fields.items()}
+        self.x = [np.ascontiguousarray(np.array(a, dtype=np.float64)) for a in (x1, x2, x3)]
+        n1, n2, n3 = self.arr["P"].shape
+        st = CCState(n1=n1, n2=n2, n3=n3)
+        for canon, attr in _CC_ATTR.items():
+            setattr(st, attr, _ptr(self.arr[canon]))
+        st.x1, st.x2, st.x3 = (_ptr(a) for a in self.x)
+        self.st = st
+        self.prm = CCParams(d1=d1, d2=d2, d3=d3, dmp=dmp, vpdt=vpdt, lr=lr, g=g, tau_C=tau_C, n_exp=n_exp, relax=relax, r=r, sh=sh)
+
+    @classmethod
+    def from_golden(cls, g, geometry: str) -> "CC":
+        names = SCRIPT_NAMES[geometry]
+        sc = eval(str(g["scalars_json"]))
+        fields = {canon: g["in_" + jn] for jn, canon in names.items()}
+        if geometry == "cylindrical":
+            x1, x2, x3 = g["coord_R_i"], g["coord_θ_i"], g["coord_Z_i"]
+            d = (sc["dr"], sc["dθ"], sc["dz"])
+            lr = sc["lr"]
+        else:
+            x1, x2, x3 = g["coord_X_i"], g["coord_Y_i"], g["coord_Z_i"]
+            d = (sc["dx"], sc["dy"], sc["dz"])
+            lr = sc["lx"]
+        return cls(geometry, fields, x1, x2, x3, d1=d[0], d2=d[1], d3=d[2], dmp=sc["dmp"], vpdt=sc["vpdt"], lr=lr,
+                   g=sc["g"], tau_C=sc["τ_C"], n_exp=sc["n_exp"], relax=sc["relax"], r=sc.get("r", 0.0), sh=sc["sh"])
+
+    def field(self, name: str) -> np.ndarray:
+        return self.arr[name]
+
+    def iterate(self, k: int = 1):
+        fn = lib().orc_cyl_iterate if self.geometry == "cylindrical" else lib().orc_cart_iterate
+        fn.argtypes = [C.POINTER(CCState), C.POINTER(CCParams), C.c_int64]
+        fn(C.byref(self.st), C.byref(self.prm), int(k))
+
+
+def golden_fields(g, geometry: str, prefix: str) -> dict:
+    """canonical-name dict of the golden arrays with the given prefix ('in_' or 'k10_' ...)"""
+    return {canon: g[prefix + jn] for jn, canon in SCRIPT_NAMES[geometry].items() if prefix + jn in g.files}

@@ -162,7 +162,7 @@ class Script:
             name = m.group(5)
             o = m.end() - 1
             c = match_paren(self.src, o)
-            params = [a.split("::")[0].strip() for a in split_args(self.src[o + 1:c])]
+            params = [_rename(a.split("::")[0].strip()) for a in split_args(self.src[o + 1:c])]
             body, _ = self._block(self.src, c + 1)
             res[name] = {"params": params, "fd": m.group(1) is None, "body": body}
         return res
@@ -237,7 +237,16 @@ def _flatten_text(body):
 
 # --------------------------------------------------------------------------
 # Julia expression -> Python/numpy
+PY_KEYWORDS = {"in", "is", "lambda", "not", "and", "or", "from", "global", "pass", "def", "class", "del", "yield", "as", "with"}
+
+
+def _rename(e: str) -> str:
+    """Julia identifiers that are Python keywords get a trailing underscore"""
+    return re.sub(r"(?<![\w.])(" + "|".join(sorted(PY_KEYWORDS)) + r")(?![\w])", r"\1_", e)
+
+
 def py_expr(e: str) -> str:
+    e = _rename(e).replace("\n", " ")
     e = e.replace("&&", " & ").replace("||", " | ").replace("^", "**").replace("π", "pi")
     # array indexing NAME[a,b,c] -> G(NAME, a, b, c)
     out, i = "", 0
@@ -284,12 +293,22 @@ def G(A, i, j, k):
     return A[i - 1, j - 1, k - 1]
 
 
-def _max(a, b):
-    return np.maximum(a, b)
+def _max(*a):
+    out = a[0]
+    for x in a[1:]:
+        out = np.maximum(out, x)
+    return out
+
+
+def _min(*a):
+    out = a[0]
+    for x in a[1:]:
+        out = np.minimum(out, x)
+    return out
 
 
 MATH = {"G": G, "pi": math.pi, "sin": np.sin, "cos": np.cos, "cot": lambda x: 1.0 / np.tan(x), "sqrt": np.sqrt,
-        "exp": np.exp, "log": np.log, "abs": np.abs, "max": _max, "min": np.minimum, "log10": math.log10,
+        "exp": np.exp, "log": np.log, "abs": np.abs, "max": _max, "min": _min, "log10": math.log10,
         "size": lambda A, d: A.shape[d - 1], "mod": lambda a, b: a % b}
 
 
@@ -302,7 +321,7 @@ class Runner:
     def _compile(self, text: str, mode="eval"):
         key = (text, mode)
         if key not in self.cache:
-            self.cache[key] = compile(text, "<jl>", mode)
+            self.cache[key] = compile(text.strip(), "<jl>", mode)
         return self.cache[key]
 
     def kernel(self, name: str, args: list[str]):
@@ -374,21 +393,31 @@ class Runner:
             if m and m.group(1) in self.s.functions:
                 self.call(m.group(1), split_args(m.group(2)))
                 continue
-            m = re.match(r"if\s+(.*)$", ln)
-            if m:
-                depth, body = 1, []
-                while depth:
-                    l2 = lines[i].strip()
-                    i += 1
-                    if re.match(r"(if|for)\b", l2) and not re.search(r"\bend\s*$", l2):
-                        depth += 1
-                    if l2 == "end":
-                        depth -= 1
-                        if depth == 0:
-                            break
-                    body.append(l2)
-                cond = re.sub(r"^\((.*)\)$", r"\1", m.group(1).strip())
-                if eval(self._compile(py_cond(cond)), MATH, self.env):
+            if re.match(r"if\b", ln):
+                if re.match(r"if\s*\(", ln):
+                    o = ln.index("(")
+                    c = match_paren(ln, o)
+                    cond, rest = ln[o + 1:c], ln[c + 1:].strip()
+                else:
+                    cond, rest = ln[2:].strip(), ""
+                if re.search(r"\bend$", rest):  # one-line `if (cond) a; b end`
+                    body = [x.strip() for x in re.sub(r"\bend$", "", rest).split(";") if x.strip()]
+                else:
+                    body = [rest] if rest else []
+                    depth = 1
+                    while True:
+                        l2 = lines[i].strip()
+                        i += 1
+                        if re.match(r"(if|for)\b", l2) and not re.search(r"\bend\s*$", l2):
+                            depth += 1
+                        if l2 == "end":
+                            depth -= 1
+                            if depth == 0:
+                                break
+                        body.append(l2)
+                body = [x for x in body if not x.startswith(("GC.", "break")) and "Base.time" not in x]
+                # convergence-check blocks (`iter % nout == 0`) only read the state; they are not replayed
+                if "nout" not in cond and eval(self._compile(py_cond(cond)), MATH, self.env):
                     self.run_lines(body)
                 continue
             m = re.match(r"(" + IDENT + r")\s*\.=\s*(" + IDENT + r")$", ln)
@@ -400,7 +429,7 @@ class Runner:
     def assign(self, ln: str):
         ln = re.sub(r"\brange\(([^()]*(?:\([^()]*\)[^()]*)*?),\s*length\s*=\s*([^()]+)\)", r"_range(\1, \2)", ln)
         ln = ln.replace("@zeros(", "_zeros(").replace("@ones(", "_ones(")
-        m = re.match(r"\((" + IDENT + r"(?:\s*,\s*" + IDENT + r")*)\)\s*=\s*\((.*)\)$", ln)
+        m = re.match(r"\(\s*(" + IDENT + r"(?:\s*,\s*" + IDENT + r")*)\s*\)\s*=\s*\((.*)\)$", ln)
         if m and " for " in m.group(2):  # coordinate comprehensions
             names = [n.strip() for n in m.group(1).split(",")]
             comps = split_args(m.group(2))
@@ -493,6 +522,10 @@ CASES = {
                    {}, {},
                    ["P", "VR", "Vθ", "VZ", "τ_RR", "τ_θθ", "τ_ZZ", "τ_Rθ", "τ_RZ", "τ_θZ", "η", "η_INI", "ηSM", "DT_R", "τII", "ρ", "η_PL"],
                    (1, 10)),
+    "cyl_diapir_pl": ("scripts_diapir/CylindricalStokes_diapir.jl", "CYL_3D_Inclusion", {"nr": 11, "nθ": 9, "nz": 7},
+                      {}, {"n_exp": 3.0},
+                      ["P", "VR", "Vθ", "VZ", "τ_RR", "τ_θθ", "τ_ZZ", "τ_Rθ", "τ_RZ", "τ_θZ", "η", "η_INI", "ηSM", "DT_R", "τII", "ρ", "η_PL"],
+                      (1, 10)),
     "cart_diapir": ("scripts_diapir/CartesianStokes_diapir.jl", "CART_3D_Inclusion_Perf", {"nx": 11, "ny": 9, "nz": 7},
                     {}, {"n_exp": 3.0},
                     ["P", "VX", "VY", "VZ", "τ_XX", "τ_YY", "τ_ZZ", "τ_XY", "τ_XZ", "τ_YZ", "η", "η_INI", "ηSM", "DT_R", "τII", "ρ", "η_PL"],
@@ -510,12 +543,14 @@ def run_case(ref: Path, name: str):
     env.update(scal)
     r = Runner(sc, env)
     # setup: everything before the PT loop (parameters, grid, allocation, initialisation)
-    for ln in setup:
-        if re.match(r"(num|runtime|err_evo|iters|t_tic|ittot)\b", ln) or ln.startswith(("print", "println")):
-            continue
-        r.run_lines([ln])
+    env["it"] = 1
+    setup = [ln for ln in setup if not (re.match(r"(num|runtime|err_evo|iters|t_tic|ittot)\b", ln) or ln.startswith(("print", "println")))]
+    r.run_lines(setup)
     env["err"] = env.get("err", 1.0)
     data = {f"in_{a}": env[a].copy() for a in save}
+    for k_, v_ in env.items():  # 1D node coordinates (range(...) results)
+        if isinstance(v_, np.ndarray) and v_.ndim == 1:
+            data[f"coord_{k_}"] = v_.copy()
     scalars = {k: float(v) for k, v in env.items() if isinstance(v, (int, float)) and not k.startswith("_")}
     done = 0
     for k in ks:

@@ -83,6 +83,9 @@ typedef enum sph_init {
                                 (SphericalStokes_diapir.jl:401-404 and the cyl/cart equivalents) */
 } sph_init;
 
+/* kernel variant of the FP32 sweeps (FP64 always uses one kernel per reference step) */
+typedef enum sph_kernels { SPH_KERNELS_AUTO = 0, SPH_KERNELS_SIMPLE = 1 } sph_kernels;
+
 /* stopping criterion of sph_solve */
 typedef enum sph_criterion {
     SPH_CRIT_REFERENCE = 0,  /* max_f max|V_f - V_f(previous iteration)| / max|V_f| < tol and iter > 20
@@ -142,7 +145,9 @@ typedef struct sph_params {
     double rho0, rho_in;   /* matrix and inclusion density */
     double radius;         /* compared with the SQUARED distance, as the reference does (:132) */
     int32_t incl_linear;   /* 1: inclusion cells are linear (phase = 1) */
-    int32_t reserved0;
+    int32_t kernels;       /* sph_kernels: FP32 sweeps fused (default) or one kernel per reference step */
+    int32_t etasm_passes;  /* passes of the 7-point max filter that gives ηSM (reference: 1; 0 means 1) */
+    int32_t reserved_i;
     double reserved[8];
 } sph_params;
 
@@ -168,6 +173,9 @@ typedef struct sph_solve_info {
     double residual;       /* final FP64 residual (SPH_CRIT_RESIDUAL definition) */
     double seconds;        /* wall time of the solve */
     int64_t nhist;         /* entries written to hist_iter / hist_err */
+    double device_ms;      /* device time of the solve (CUDA events on the context's stream) */
+    double sweep_ms;       /* of which PT sweeps (MIXED: the FP32 correction sweeps) */
+    double outer_ms;       /* of which FP64 outer work (MIXED: residual, coefficients) */
 } sph_solve_info;
 
 /* defaults of the reference script of the given geometry (diapir setups) */
@@ -193,6 +201,14 @@ int sph_step(void* ctx, int64_t k);
 /* iterate to the tolerance; hist_* (may be NULL) receive up to hist_cap (iter, err) pairs */
 int sph_solve(void* ctx, const sph_solve_opts* opts, sph_solve_info* info,
               int64_t* hist_iter, double* hist_err, int64_t hist_cap);
+
+/* MIXED only: k FP32 PT sweeps of the current defect-correction step (the hot path of
+ * sph_solve).  The first call after the FP64 state changed prepares the step (FP64
+ * residual, frozen viscosity, zero correction) outside the timed region;
+ * sph_last_device_ms() then returns the device time of the k sweeps.
+ * sph_sweep_apply() adds the correction to the FP64 state and ends the step. */
+int sph_sweep(void* ctx, int64_t k);
+int sph_sweep_apply(void* ctx);
 
 /* FP64 Stokes residual of the current state: out[0..2] max|R_mom| per component,
  * out[3] max|div V|, out[4] max|V|, out[5] f_scale, out[6] the SPH_CRIT_RESIDUAL error */

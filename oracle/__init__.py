@@ -32,7 +32,8 @@ class SphState(C.Structure):
 
 class SphParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("_dr", "_dt", "_dp", "dmp", "vpdt", "lr", "g", "tau_C", "n_exp", "r", "sh")] + [
-        ("bc", C.c_int32), ("rheo", C.c_int32)] + [(n, C.c_double) for n in ("relax", "edot_bg", "sig_t", "sig_p")]
+        ("bc", C.c_int32), ("rheo", C.c_int32)] + [(n, C.c_double) for n in ("relax", "edot_bg", "sig_t", "sig_p")] + [
+        ("passes", C.c_int32), ("pad_", C.c_int32)]
 
 
 _lib = None
@@ -87,7 +88,7 @@ class Sph:
              "DT_R": "DT_R", "TII": "tII", "RHO": "rho"}
 
     def __init__(self, nr, nt, np_, *, r, c2, lr, lt, lp, l_ref, dmp, vpdt, g, tau_C, n_exp, sh, bc, rheo,
-                 relax=0.5, edot_bg=1.0, sig_t=0.0, sig_p=0.0, c1=None, c3=0.0):
+                 relax=0.5, edot_bg=1.0, sig_t=0.0, sig_p=0.0, c1=None, c3=0.0, passes=1):
         self.n = (nr, nt, np_)
         c1 = r if c1 is None else c1
         z = lambda *s: np.zeros(s, dtype=np.float64, order="F")
@@ -106,7 +107,7 @@ class Sph:
         self.eta_tmp = np.zeros(nr * nt * np_ + int(lib().orc_sph_scratch_size(nr, nt, np_)), dtype=np.float64)
         self.prm = SphParams(_dr=(nr - 1) / lr, _dt=(nt - 1) / lt, _dp=(np_ - 1) / lp, dmp=dmp, vpdt=vpdt, lr=l_ref,
                              g=g, tau_C=tau_C, n_exp=n_exp, r=r, sh=sh, bc=bc, rheo=rheo, relax=relax,
-                             edot_bg=edot_bg, sig_t=sig_t, sig_p=sig_p)
+                             edot_bg=edot_bg, sig_t=sig_t, sig_p=sig_p, passes=passes)
         self._sync()
 
     def _sync(self):
@@ -124,7 +125,7 @@ class Sph:
         o = cls(p.n1, p.n2, p.n3, r=p.r, c1=p.c1, c2=p.c2, c3=p.c3, lr=p.l1, lt=p.l2, lp=p.l3, l_ref=p.l_ref,
                 dmp=p.dmp, vpdt=p.vpdt if p.vpdt > 0 else p.l1 / (p.n1 - 1) / (2.0 + 4.5 * math.log10(p.vr)),
                 g=p.g, tau_C=p.tau_C, n_exp=p.n_exp, sh=p.sh, bc=p.bc, rheo=rheo, relax=p.relax,
-                edot_bg=p.edot_bg, sig_t=p.sig_bc[1], sig_p=p.sig_bc[2])
+                edot_bg=p.edot_bg, sig_t=p.sig_bc[1], sig_p=p.sig_bc[2], passes=max(1, p.etasm_passes))
         o.rho[:] = p.rho0
         o.eta[:] = p.eta0
         if p.init == 1:
@@ -173,9 +174,17 @@ class Sph:
         nr, nt, np_ = self.n
         lib().orc_maxloc(_ptr(self.etaSM), _ptr(self.eta), nr, nt, np_)
         lib().orc_copy_BC(_ptr(self.etaSM), nr, nt, np_)
+        for _ in range(self.prm.passes - 1):
+            tmp = self.etaSM.copy(order="F")
+            lib().orc_maxloc(_ptr(self.etaSM), _ptr(tmp), nr, nt, np_)
+            lib().orc_copy_BC(_ptr(self.etaSM), nr, nt, np_)
 
     def compute_P(self):
         lib().orc_sph_compute_P(C.byref(self.st), C.byref(self.prm))
+        if self.prm.bc == 2:
+            L = lib()
+            L.orc_sph_stress_pressure.argtypes = [_PD, _PD, _PD, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double]
+            L.orc_sph_stress_pressure(_ptr(self.P), _ptr(self.ttt), _ptr(self.tpp), *self.n, self.prm.sig_t, self.prm.sig_p)
 
     def power_law(self):
         nr, nt, np_ = self.n

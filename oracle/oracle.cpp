@@ -26,6 +26,7 @@
 #include <cstdint>
 #include <cstring>
 #include <algorithm>
+#include <vector>
 
 #if defined(_OPENMP)
 #include <omp.h>
@@ -44,6 +45,8 @@ struct Arr {
 };
 
 inline double cot(double x) { return 1.0 / std::tan(x); }  // Base.cot = inv(tan(x))
+// max of |x| that propagates NaN (a norm of a diverged state must not read 0)
+inline double nmax(double m, double x) { x = std::fabs(x); return (x != x || m != m) ? NAN : (x > m ? x : m); }
 inline double sq(double x) { return x * x; }
 
 }  // namespace
@@ -73,6 +76,8 @@ struct orc_sph_params {
     int32_t rheo;          // 0 stress power law (:259-265), 1 EXT strain-rate power law, 2 linear (skip)
     double relax, edot_bg; // EXT
     double sig_t, sig_p;   // EXT far-field normal stresses on the theta / phi faces
+    int32_t passes;        // EXT applications of the 7-point max filter giving ηSM (reference: 1)
+    int32_t pad_;
 };
 
 static inline Arr A(double* p, long n1, long n2, long n3) { return Arr{p, n1, n2, n3}; }
@@ -344,13 +349,16 @@ static void sph_bc_p_free(orc_sph_state* s, bool copy_normal_ghost = true) {
         for (long j = 1; j <= nt; ++j) for (long i = 1; i <= nr; ++i) { Vp(i, j, 1) = -Vp(i, j, 2); Vp(i, j, np + 1) = -Vp(i, j, np); }
 }
 
-// EXT far-field normal stress: the ghost normal velocity is chosen so that the
-// boundary cell's total normal stress -P + 2 η D_nn equals the prescribed
-// value (D_nn deviatoric, as in compute_P!).  Tangential components: free slip.
+// EXT far-field normal stress (classic free-surface treatment of a grid whose
+// boundary cells are centred on the wall): the ghost normal velocity makes the
+// boundary cell divergence-free, and the boundary cell's pressure is slaved to
+// the traction, P = τ_nn - σ_bc (sph_stress_pressure, after compute_P!; the
+// average of the two conditions at cells on both a θ and a φ face).
+// Tangential components: free slip.
 static void sph_bc_stress_t(orc_sph_state* s, const orc_sph_params* q) {
     const long nr = s->nr, nt = s->nt, np = s->np;
     Arr VR = A(s->VR, nr + 1, nt, np), Vt = A(s->Vt, nr, nt + 1, np), Vp = A(s->Vp, nr, nt, np + 1);
-    Arr P = A(s->P, nr, nt, np), eta = A(s->eta, nr, nt, np), R = A(s->R, nr, nt, np), th = A(s->th, nr, nt, np);
+    Arr R = A(s->R, nr, nt, np), th = A(s->th, nr, nt, np);
     const double _dr = q->_dr, _dt = q->_dt, _dp = q->_dp;
     for (int side = 0; side < 2; ++side) {
         long jb = side == 0 ? 1 : nt;          // boundary cell row
@@ -360,25 +368,21 @@ static void sph_bc_stress_t(orc_sph_state* s, const orc_sph_params* q) {
         for (long k = 1; k <= np; ++k)
             for (long i = 1; i <= nr; ++i) {
                 double Rc = R(i, jb, k), tc = th(i, jb, k);
-                double a1 = _dr, a2 = _dt / Rc, a3 = _dp / (Rc * std::sin(tc));
-                double c1 = 2.0 / Rc, c2 = cot(tc) / Rc, e1 = 1.0 / Rc;
+                double a2 = _dt / Rc, a3 = _dp / (Rc * std::sin(tc)), c1 = 2.0 / Rc, c2 = cot(tc) / Rc;
                 double avx = 0.5 * (VR(i, jb, k) + VR(i + 1, jb, k));
                 double v = Vt(i, jv, k);
-                // DIVV = A0 + B*g ; D_tt = C0 + Cg*g
-                double A0 = a1 * (VR(i + 1, jb, k) - VR(i, jb, k)) + a3 * (Vp(i, jb, k + 1) - Vp(i, jb, k)) + c1 * avx +
-                            a2 * (-sgn) * v + c2 * 0.5 * v;
+                // DIVV = A0 + B*ghost = 0
+                double A0 = _dr * (VR(i + 1, jb, k) - VR(i, jb, k)) + a3 * (Vp(i, jb, k + 1) - Vp(i, jb, k)) + c1 * avx + a2 * (-sgn) * v + c2 * 0.5 * v;
                 double B = a2 * sgn + 0.5 * c2;
-                double C0 = a2 * (-sgn) * v + e1 * avx - A0 / 3.0;
-                double Cg = a2 * sgn - B / 3.0;
-                double Dt = (q->sig_t + P(i, jb, k)) / (2.0 * eta(i, jb, k));
-                Vt(i, jg, k) = (Dt - C0) / Cg;
+                Vt(i, jg, k) = -A0 / B;
             }
     }
+    (void)q;
 }
 static void sph_bc_stress_p(orc_sph_state* s, const orc_sph_params* q) {
     const long nr = s->nr, nt = s->nt, np = s->np;
     Arr VR = A(s->VR, nr + 1, nt, np), Vt = A(s->Vt, nr, nt + 1, np), Vp = A(s->Vp, nr, nt, np + 1);
-    Arr P = A(s->P, nr, nt, np), eta = A(s->eta, nr, nt, np), R = A(s->R, nr, nt, np), th = A(s->th, nr, nt, np);
+    Arr R = A(s->R, nr, nt, np), th = A(s->th, nr, nt, np);
     const double _dr = q->_dr, _dt = q->_dt, _dp = q->_dp;
     for (int side = 0; side < 2; ++side) {
         long kb = side == 0 ? 1 : np, kg = side == 0 ? 1 : np + 1, kv = side == 0 ? 2 : np;
@@ -386,20 +390,31 @@ static void sph_bc_stress_p(orc_sph_state* s, const orc_sph_params* q) {
         for (long j = 1; j <= nt; ++j)
             for (long i = 1; i <= nr; ++i) {
                 double Rc = R(i, j, kb), tc = th(i, j, kb);
-                double a1 = _dr, a2 = _dt / Rc, a3 = _dp / (Rc * std::sin(tc));
-                double c1 = 2.0 / Rc, c2 = cot(tc) / Rc, e1 = 1.0 / Rc, e2 = cot(tc) / Rc;
+                double a2 = _dt / Rc, a3 = _dp / (Rc * std::sin(tc)), c1 = 2.0 / Rc, c2 = cot(tc) / Rc;
                 double avx = 0.5 * (VR(i, j, kb) + VR(i + 1, j, kb));
                 double avy = 0.5 * (Vt(i, j, kb) + Vt(i, j + 1, kb));
                 double v = Vp(i, j, kv);
-                double A0 = a1 * (VR(i + 1, j, kb) - VR(i, j, kb)) + a2 * (Vt(i, j + 1, kb) - Vt(i, j, kb)) + c1 * avx + c2 * avy +
-                            a3 * (-sgn) * v;
+                double A0 = _dr * (VR(i + 1, j, kb) - VR(i, j, kb)) + a2 * (Vt(i, j + 1, kb) - Vt(i, j, kb)) + c1 * avx + c2 * avy + a3 * (-sgn) * v;
                 double B = a3 * sgn;
-                double C0 = a3 * (-sgn) * v + e1 * avx + e2 * avy - A0 / 3.0;
-                double Cg = a3 * sgn - B / 3.0;
-                double Dt = (q->sig_p + P(i, j, kb)) / (2.0 * eta(i, j, kb));
-                Vp(i, j, kg) = (Dt - C0) / Cg;
+                Vp(i, j, kg) = -A0 / B;
             }
     }
+}
+
+// EXT: boundary-cell pressure of the stress BC, P = τ_nn - σ_bc on the θ and φ faces
+void orc_sph_stress_pressure(double* Pa, const double* ttt, const double* tpp, int64_t nr, int64_t nt, int64_t np,
+                             double sig_t, double sig_p) {
+    Arr P = A(Pa, nr, nt, np), T2 = A(const_cast<double*>(ttt), nr, nt, np), T3 = A(const_cast<double*>(tpp), nr, nt, np);
+    for (long k = 1; k <= np; ++k)
+        for (long j = 1; j <= nt; ++j)
+            for (long i = 1; i <= nr; ++i) {
+                bool bt = (j == 1 || j == nt), bp = (k == 1 || k == np);
+                if (!bt && !bp) continue;
+                double acc = 0.0, cnt = 0.0;
+                if (bt) { acc += T2(i, j, k) - sig_t; cnt += 1.0; }
+                if (bp) { acc += T3(i, j, k) - sig_p; cnt += 1.0; }
+                P(i, j, k) = acc / cnt;
+            }
 }
 
 void orc_sph_apply_bc(orc_sph_state* s, const orc_sph_params* q) {
@@ -506,7 +521,13 @@ void orc_sph_iterate(orc_sph_state* s, const orc_sph_params* q, int64_t niter) {
         orc_sph_equal3(s);
         orc_maxloc(s->etaSM, s->eta, nr, nt, np);
         orc_copy_BC(s->etaSM, nr, nt, np);
+        for (int pass = 1; pass < q->passes; ++pass) {  // EXT wider max filter
+            std::vector<double> tmp(s->etaSM, s->etaSM + nr * nt * np);
+            orc_maxloc(s->etaSM, tmp.data(), nr, nt, np);
+            orc_copy_BC(s->etaSM, nr, nt, np);
+        }
         orc_sph_compute_P(s, q);
+        if (q->bc == 2) orc_sph_stress_pressure(s->P, s->ttt, s->tpp, nr, nt, np, q->sig_t, q->sig_p);
         if (q->rheo == 0) {
             orc_sph_compute_TII(s);
             orc_copy_BC(s->tII, nr, nt, np);
@@ -536,8 +557,8 @@ double orc_sph_check_err(orc_sph_state* s) {
         double md = 0.0, mv = 0.0;
         for (long c = 0; c < n[f]; ++c) {
             E[f][c] = V[f][c] - E[f][c];
-            md = std::max(md, std::fabs(E[f][c]));
-            mv = std::max(mv, std::fabs(V[f][c]));
+            md = nmax(md, E[f][c]);
+            mv = nmax(mv, V[f][c]);
         }
         err = std::max(err, md / mv);
     }
@@ -574,7 +595,7 @@ void orc_sph_residual(orc_sph_state* s, const orc_sph_params* q, double* out, do
         Arr DIV = A(rDiv ? rDiv : DT_R, nr, nt, np);
         const double _dr = q->_dr, _dt = q->_dt, _dp = q->_dp;
         double mdiv = 0.0;
-#pragma omp parallel for schedule(static) reduction(max : mdiv)
+#pragma omp parallel for schedule(static)
         for (long k = 1; k <= np; ++k)
             for (long j = 1; j <= nt; ++j)
                 for (long i = 1; i <= nr; ++i) {
@@ -589,7 +610,6 @@ void orc_sph_residual(orc_sph_state* s, const orc_sph_params* q, double* out, do
                     double e = E(i, j, k);
                     TRR(i, j, k) = 2.0 * e * DRR; TTT(i, j, k) = 2.0 * e * Dtt; TPP(i, j, k) = 2.0 * e * Dpp;
                     DIV(i, j, k) = DIVV;
-                    mdiv = std::max(mdiv, std::fabs(DIVV));
                     if (i <= nr - 1 && j <= nt - 1 && k <= np - 2) {
                         double aR = ((R(i, j, k + 1) + R(i, j + 1, k + 1) + R(i + 1, j, k + 1) + R(i + 1, j + 1, k + 1)) * 0.25);
                         double D = (Vt(i + 1, j + 1, k + 1) - Vt(i, j + 1, k + 1)) * _dr + 1.0 / aR * (VR(i + 1, j + 1, k + 1) - VR(i + 1, j, k + 1)) * _dt -
@@ -614,11 +634,19 @@ void orc_sph_residual(orc_sph_state* s, const orc_sph_params* q, double* out, do
                         Ttp(i, j, k) = aE * D;
                     }
                 }
+        const double* dv = rDiv ? rDiv : DT_R;
+        for (long c = 0; c < nc; ++c) mdiv = nmax(mdiv, dv[c]);
         out[3] = mdiv;
     }
     // momentum residual: compute_V! increments with DT_R = 1 into zeroed arrays
     orc_sph_state t = *s;
     t.tRR = tRR; t.ttt = ttt; t.tpp = tpp; t.tRt = tRt; t.tRp = tRp; t.ttp = ttp;
+    std::vector<double> Pres;
+    if (q->bc == 2) {  // boundary-cell pressure of the stress BC from the viscous stresses
+        Pres.assign(s->P, s->P + nc);
+        orc_sph_stress_pressure(Pres.data(), ttt, tpp, nr, nt, np, q->sig_t, q->sig_p);
+        t.P = Pres.data();
+    }
     long nv[3] = {(nr + 1) * nt * np, nr * (nt + 1) * np, nr * nt * (np + 1)};
     double* own[3] = {rVR, rVt, rVp};
     double* tmp[3];
@@ -632,7 +660,7 @@ void orc_sph_residual(orc_sph_state* s, const orc_sph_params* q, double* out, do
     for (int f = 0; f < 3; ++f) {
         double m = 0.0, mv = 0.0;
         double* V = f == 0 ? s->VR : (f == 1 ? s->Vt : s->Vp);
-        for (long c = 0; c < nv[f]; ++c) { m = std::max(m, std::fabs(tmp[f][c])); mv = std::max(mv, std::fabs(V[c])); }
+        for (long c = 0; c < nv[f]; ++c) { m = nmax(m, tmp[f][c]); mv = nmax(mv, V[c]); }
         out[f] = m;
         out[4] = f == 0 ? mv : std::max(out[4], mv);
         if (!own[f]) delete[] tmp[f];

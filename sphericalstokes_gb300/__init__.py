@@ -32,6 +32,7 @@ PREC = {"fp64": 0, "fp32": 1, "mixed": 2}
 BC = {"diapir": 0, "free_slip": 1, "stress": 2}
 RHEO = {"linear": 0, "tau_power": 1, "tau_power_relax": 2, "edot_power_relax": 3}
 INIT = {"none": 0, "inclusion": 1}
+KERNELS_VARIANT = {"auto": 0, "simple": 1}
 CRIT = {"reference": 0, "residual": 1}
 FIELDS = {
     "P": 0, "V1": 1, "V2": 2, "V3": 3, "TAU11": 4, "TAU22": 5, "TAU33": 6,
@@ -64,7 +65,8 @@ class Params(C.Structure):
         ("relax", C.c_double), ("edot_bg", C.c_double), ("r", C.c_double), ("sh", C.c_double),
         ("sig_bc", C.c_double * 3),
         ("eta0", C.c_double), ("vr", C.c_double), ("rho0", C.c_double), ("rho_in", C.c_double),
-        ("radius", C.c_double), ("incl_linear", C.c_int32), ("reserved0", C.c_int32),
+        ("radius", C.c_double), ("incl_linear", C.c_int32), ("kernels", C.c_int32),
+        ("etasm_passes", C.c_int32), ("reserved_i", C.c_int32),
         ("reserved", C.c_double * 8),
     ]
 
@@ -81,6 +83,7 @@ class SolveInfo(C.Structure):
     _fields_ = [
         ("iters", C.c_int64), ("outer", C.c_int32), ("status", C.c_int32), ("err", C.c_double),
         ("residual", C.c_double), ("seconds", C.c_double), ("nhist", C.c_int64),
+        ("device_ms", C.c_double), ("sweep_ms", C.c_double), ("outer_ms", C.c_double),
     ]
 
 
@@ -98,6 +101,8 @@ _SIGS = {
     "sph_solve": ([C.c_void_p, C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.POINTER(C.c_int64),
                    C.POINTER(C.c_double), C.c_int64], C.c_int),
     "sph_residual": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
+    "sph_sweep": ([C.c_void_p, C.c_int64], C.c_int),
+    "sph_sweep_apply": ([C.c_void_p], C.c_int),
     "sph_run_kernel": ([C.c_void_p, C.c_int32], C.c_int),
     "sph_last_device_ms": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "sph_strerror": ([C.c_int], C.c_char_p),
@@ -146,7 +151,7 @@ def default_params(geometry: str = "spherical", **kw) -> Params:
 
 
 def set_params(p: Params, **kw) -> Params:
-    enums = {"geometry": GEOM, "precision": PREC, "bc": BC, "rheology": RHEO, "init": INIT}
+    enums = {"geometry": GEOM, "precision": PREC, "bc": BC, "rheology": RHEO, "init": INIT, "kernels": KERNELS_VARIANT}
     for k, v in kw.items():
         if k in enums and isinstance(v, str):
             v = enums[k][v]
@@ -177,6 +182,9 @@ class SolveResult:
     seconds: float
     hist_iter: np.ndarray
     hist_err: np.ndarray
+    device_ms: float = 0.0
+    sweep_ms: float = 0.0
+    outer_ms: float = 0.0
 
     @property
     def converged(self) -> bool:
@@ -277,7 +285,16 @@ class Solver:
             _check(self.lib, rc, "sph_solve")
         n = int(info.nhist)
         return SolveResult(int(info.status), int(info.iters), int(info.outer), float(info.err), float(info.residual),
-                           float(info.seconds), hi[:n].copy(), he[:n].copy())
+                           float(info.seconds), hi[:n].copy(), he[:n].copy(), float(info.device_ms), float(info.sweep_ms),
+                           float(info.outer_ms))
+
+    def sweep(self, k: int) -> float:
+        """k FP32 sweeps of the current defect-correction step (MIXED); returns their device time in ms."""
+        _check(self.lib, self.lib.sph_sweep(self._h, int(k)), "sph_sweep")
+        return self.last_device_ms()
+
+    def sweep_apply(self) -> None:
+        _check(self.lib, self.lib.sph_sweep_apply(self._h), "sph_sweep_apply")
 
     def residual(self) -> dict:
         out = (C.c_double * 7)()

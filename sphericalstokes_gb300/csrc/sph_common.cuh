@@ -64,10 +64,24 @@ struct KP {
     T g;
     T tau_C, n_exp, relax, edot_bg;
     T sig2, sig3;                      // prescribed total normal stress on x2 / x3 faces
+    int traction;                      // 1: boundary cells on x2/x3 faces take P = τ_nn - σ_bc
     unsigned long long* red;           // reduction slots (max of |x| as ordered bits)
 };
 
 __host__ __device__ inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// pressure of a boundary cell under the far-field normal-stress BC: the total
+// normal stress -P + τ_nn equals the prescribed σ on the x2 faces (j = 0, n2-1)
+// and x3 faces (k = 0, n3-1); the average of both conditions on cells of both.
+// Returns false (P unchanged) for cells on no such face.
+template <typename T>
+__device__ __forceinline__ bool traction_pressure(int j, int k, int n2, int n3, T t22, T t33, T sig2, T sig3, T& P) {
+    const bool b2 = (j == 0 || j == n2 - 1), b3 = (k == 0 || k == n3 - 1);
+    if (!b2 && !b3) return false;
+    if (b2 && b3) P = ((t22 - sig2) + (t33 - sig3)) / T(2);
+    else P = b2 ? (t22 - sig2) : (t33 - sig3);
+    return true;
+}
 
 // order-preserving bits of a non-negative double (NaN maps above +inf)
 __device__ __forceinline__ unsigned long long ord_bits(double x) { return (unsigned long long)__double_as_longlong(x); }

@@ -1,0 +1,243 @@
+// Fused FP32 PT sweep: compute_P! and compute_V! of one PT iteration in a
+// single launch (SphericalStokes_diapir.jl:416-422), bandwidth-bound design.
+//
+// A block owns a TX x TY column of cells in (x1, x2) and marches along x3
+// over a chunk of planes (2.5D blocking).  Per plane K it
+//   1. issues asynchronous copies (cp.async, Ampere-style LDGSTS) of the input
+//      plane K+2 (V1, V2, V3, η, ηSM on the tile + halo) into a 3-slot ring, and
+//      of the old P, τ (and rP or ρ) of plane K+1 plus the right-hand side rV
+//      of plane K+1 into 2-slot rings, so DRAM latency overlaps the compute of
+//      plane K;
+//   2. updates P, τ11..τ33 (cells) and τ12, τ13, τ23 (edges) of plane K on the
+//      tile plus a one-point halo on the low x1/x2 sides (one point per thread:
+//      (TX+1)(TY+1) <= threads), keeping them in a 2-plane shared ring and
+//      writing the owned points to the output state;
+//   3. updates V1, V2, V3 of plane K from the shared stresses of planes K-1, K.
+// Every state field is read once and written once per sweep (halo re-reads
+// hit L2); the old and new states are different buffers (ping-pong) and the
+// boundary-condition stages run afterwards on the new state.  The arithmetic
+// is the shared core of sph_core.cuh: results equal those of k_stress +
+// k_velocity.
+//
+// MODE 0: reference iteration (ρg body force).  MODE 1: correction problem of
+// the mixed-precision solve (right-hand sides rP, rV; η and ηSM frozen).
+#pragma once
+#include "sph_core.cuh"
+
+namespace sph {
+
+template <typename T>
+struct FusedOut {
+    T *P, *V1, *V2, *V3, *t11, *t22, *t33, *t12, *t13, *t23;
+};
+
+constexpr int FTX = 32, FTY = 8;                  // owned tile (cells) per block
+constexpr int FLX = FTX + 2, FLY = FTY + 2;       // input tile with halo
+constexpr int FSX = FTX + 1, FSY = FTY + 1;       // stage-1 points (tile + low halo)
+constexpr int FNT = 320;                          // threads: >= FSX*FSY = 297 and a multiple of 32
+constexpr int F_IN = 5;                           // V1 V2 V3 η ηSM
+constexpr int F_OLD = 8;                          // P τ11 τ22 τ33 τ12 τ13 τ23 + (rP | ρ)
+constexpr int F_RV = 3;                           // rV1 rV2 rV3
+
+struct FusedSmem {
+    float in[3][F_IN][FLY][FLX];    // input ring (planes K, K+1, K+2)
+    float old[2][F_OLD][FSY][FSX];  // old state ring (planes K, K+1)
+    float rv[2][F_RV][FTY][FTX];    // right-hand side ring (planes K, K+1)
+    float st[2][8][FSY][FSX];       // new stresses ring (planes K-1, K): P t11 t22 t33 t12 t13 t23 DT_R
+};
+
+__device__ __forceinline__ void cp_async4(float* smem, const float* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int sz = valid ? 4 : 0;  // 0: zero-fill, nothing read
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(s), "l"(gmem), "r"(sz) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int G, int MODE>
+__global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o, int kchunk) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    FusedSmem& S = *reinterpret_cast<FusedSmem*>(smem_raw);
+    enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-ring / stress-ring field slots (IX: rP | ρ, or DT_R)
+
+    const Dims d = p.d;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * FTY;
+    const int kA = blockIdx.z * kchunk;
+    const int kB = min(kA + kchunk, d.n3);
+    const int n1 = d.n1, n2 = d.n2, n3 = d.n3;
+    const float d1 = p.d1, d2 = p.d2, d3 = p.d3, gsc = p.gsc, kbc = p.kbc, vpdt2 = p.vpdt2;
+    if (kA >= kB) return;
+
+    // asynchronous loads of one plane (zero fill outside the box / for z outside [0, pz))
+    auto issue_inputs = [&](int z) {
+        const int sl = ((z % 3) + 3) % 3;
+        const bool zok = z >= 0 && z < d.pz;
+        for (int q = tid; q < FLX * FLY; q += FNT) {
+            const int lx = q % FLX, ly = q / FLX;
+            const int x = x0 - 1 + lx, y = y0 - 1 + ly;
+            const bool ok = zok && x >= 0 && x < d.px && y >= 0 && y < d.py;
+            const int g = ok ? x + d.sy * y + d.sz * z : 0;
+            cp_async4(&S.in[sl][0][ly][lx], p.V1 + g, ok);
+            cp_async4(&S.in[sl][1][ly][lx], p.V2 + g, ok);
+            cp_async4(&S.in[sl][2][ly][lx], p.V3 + g, ok);
+            cp_async4(&S.in[sl][3][ly][lx], p.eta + g, ok);
+            cp_async4(&S.in[sl][4][ly][lx], p.etaSM + g, ok);
+        }
+    };
+    auto issue_old = [&](int z) {
+        const int sl = z & 1;
+        if (tid < FSX * FSY) {
+            const int a = tid % FSX, b = tid / FSX;
+            const int x = x0 - 1 + a, y = y0 - 1 + b;
+            const bool ok = z >= 0 && z < d.n3 && x >= 0 && x < d.n1 && y >= 0 && y < d.n2;
+            const int g = ok ? x + d.sy * y + d.sz * z : 0;
+            cp_async4(&S.old[sl][IP][b][a], p.P + g, ok);
+            cp_async4(&S.old[sl][I11][b][a], p.t11 + g, ok);
+            cp_async4(&S.old[sl][I22][b][a], p.t22 + g, ok);
+            cp_async4(&S.old[sl][I33][b][a], p.t33 + g, ok);
+            cp_async4(&S.old[sl][I12][b][a], p.t12 + g, ok);
+            cp_async4(&S.old[sl][I13][b][a], p.t13 + g, ok);
+            cp_async4(&S.old[sl][I23][b][a], p.t23 + g, ok);
+            cp_async4(&S.old[sl][IX][b][a], (MODE == 1 ? p.rP : p.rho) + g, ok);
+        }
+    };
+    auto issue_rv = [&](int z) {
+        if (MODE != 1) return;
+        const int sl = z & 1;
+        if (tid < FTX * FTY) {
+            const int a = tid % FTX, b = tid / FTX;
+            const int x = x0 + a, y = y0 + b;
+            const bool ok = z >= 0 && z < d.pz && x < d.px && y < d.py;
+            const int g = ok ? x + d.sy * y + d.sz * z : 0;
+            cp_async4(&S.rv[sl][0][b][a], p.rV1 + g, ok);
+            cp_async4(&S.rv[sl][1][b][a], p.rV2 + g, ok);
+            cp_async4(&S.rv[sl][2][b][a], p.rV3 + g, ok);
+        }
+    };
+
+    // stresses of plane k at this thread's stage-1 point; owned points go to the output state
+    auto stage1 = [&](int k, bool own_plane) {
+        if (tid >= FSX * FSY) return;
+        const int ik = ((k % 3) + 3) % 3, ik1 = (((k + 1) % 3) + 3) % 3, so = k & 1, ol = k & 1;
+        const int a = tid % FSX, b = tid / FSX;
+        const int x = x0 - 1 + a, y = y0 - 1 + b;
+        const bool own = own_plane && a >= 1 && b >= 1;
+        const int g = x + d.sy * y + d.sz * k;
+        float (*I0)[FLY][FLX] = S.in[ik];
+        float (*I1)[FLY][FLX] = S.in[ik1];
+        float (*O)[FSY][FSX] = S.old[ol];
+        float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
+        if (x >= 0 && y >= 0 && x < n1 && y < n2) {
+            {
+                const CellD<float> D = cell_strain<float, G>(p.geo, d1, d2, d3, x, y, I0[0][b][a], I0[0][b][a + 1], I0[1][b][a], I0[1][b + 1][a],
+                                                             I0[2][b][a], I1[2][b][a]);
+                const float sm = I0[4][b][a], e = I0[3][b][a];
+                const float gs = gsc * sm, kb = kbc * sm;
+                const float f = e / (e + gs);
+                float dv = D.div;
+                if (MODE == 1) dv += O[IX][b][a];
+                vP = O[IP][b][a] - kb * dv;
+                v11 = (O[I11][b][a] + 2.f * gs * D.D11) * f;
+                v22 = (O[I22][b][a] + 2.f * gs * D.D22) * f;
+                v33 = (O[I33][b][a] + 2.f * gs * D.D33) * f;
+                if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
+                vdt = vpdt2 / (kb + gs * f);
+                if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
+            }
+            if (x < n1 - 1 && y < n2 - 1 && k < n3 - 2) {
+                const float D = edge12<float, G>(p.geo, d1, d2, x, I1[1][b + 1][a], I1[1][b + 1][a + 1], I1[0][b][a + 1], I1[0][b + 1][a + 1]);
+                v12 = edge_update(O[I12][b][a], gsc, I1[4][b][a] + I1[4][b + 1][a] + I1[4][b][a + 1] + I1[4][b + 1][a + 1],
+                                  I1[3][b][a] + I1[3][b + 1][a] + I1[3][b][a + 1] + I1[3][b + 1][a + 1], D);
+                if (own) o.t12[g] = v12;
+            }
+            if (x < n1 - 1 && y < n2 - 2 && k < n3 - 1) {
+                const float D = edge13<float, G>(p.geo, d1, d3, x, y, I1[2][b + 1][a], I1[2][b + 1][a + 1], I0[0][b + 1][a + 1], I1[0][b + 1][a + 1]);
+                v13 = edge_update(O[I13][b][a], gsc, I0[4][b + 1][a] + I1[4][b + 1][a] + I0[4][b + 1][a + 1] + I1[4][b + 1][a + 1],
+                                  I0[3][b + 1][a] + I1[3][b + 1][a] + I0[3][b + 1][a + 1] + I1[3][b + 1][a + 1], D);
+                if (own) o.t13[g] = v13;
+            }
+            if (x < n1 - 2 && y < n2 - 1 && k < n3 - 1) {
+                const float D = edge23<float, G>(p.geo, d2, d3, x, y, I1[2][b][a + 1], I1[2][b + 1][a + 1], I0[1][b + 1][a + 1], I1[1][b + 1][a + 1]);
+                v23 = edge_update(O[I23][b][a], gsc, I0[4][b][a + 1] + I1[4][b][a + 1] + I0[4][b + 1][a + 1] + I1[4][b + 1][a + 1],
+                                  I0[3][b][a + 1] + I1[3][b][a + 1] + I0[3][b + 1][a + 1] + I1[3][b + 1][a + 1], D);
+                if (own) o.t23[g] = v23;
+            }
+        }
+        float (*W)[FSY][FSX] = S.st[so];
+        W[IP][b][a] = vP; W[I11][b][a] = v11; W[I22][b][a] = v22; W[I33][b][a] = v33;
+        W[I12][b][a] = v12; W[I13][b][a] = v13; W[I23][b][a] = v23; W[IX][b][a] = vdt;
+    };
+
+    // velocities of plane K from the stresses of planes K-1 and K
+    auto velocity = [&](int K) {
+        if (tid >= FTX * FTY) return;
+        const int tx = tid % FTX, ty = tid / FTX;
+        const int I = x0 + tx, J = y0 + ty;
+        if (I < 1 || J < 1 || K < 1 || I > n1 - 1 || J > n2 - 1 || K > n3 - 1) return;
+        const int g = I + d.sy * J + d.sz * K;
+        const float h = 0.5f;
+        float (*C0)[FSY][FSX] = S.st[K & 1];
+        float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
+        float (*Vin)[FLY][FLX] = S.in[K % 3];
+        const float Pc = C0[IP][ty + 1][tx + 1];
+        const float q11 = C0[I11][ty + 1][tx + 1] - Pc, q22 = C0[I22][ty + 1][tx + 1] - Pc, q33 = C0[I33][ty + 1][tx + 1] - Pc;
+        const float dtc = C0[IX][ty + 1][tx + 1];
+        if (J <= n2 - 2 && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
+            const float Pm = C0[IP][ty + 1][tx];
+            float r = mom1<float, G>(p.geo, d1, d2, d3, I, J, C0[I11][ty + 1][tx] - Pm, q11, C0[I22][ty + 1][tx] - Pm, q22, C0[I33][ty + 1][tx] - Pm,
+                                     q33, C1[I12][ty + 1][tx], C1[I12][ty][tx], C0[I13][ty][tx], C1[I13][ty][tx]);
+            if (G != CART && MODE == 0) {
+                const float* rho = &S.old[K & 1][IX][0][0];
+                r -= (rho[(ty + 1) * FSX + tx] * p.g + rho[(ty + 1) * FSX + tx + 1] * p.g) * h;
+            }
+            if (MODE == 1) r += S.rv[K & 1][0][ty][tx];
+            o.V1[g] = Vin[0][ty + 1][tx + 1] + r * ((C0[IX][ty + 1][tx] + dtc) * h);
+        }
+        if (I <= n1 - 2 && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
+            const float Pm = C0[IP][ty][tx + 1];
+            float r = mom2<float, G>(p.geo, d1, d2, d3, I, J, C0[I22][ty][tx + 1] - Pm, q22, C0[I33][ty][tx + 1] - Pm, q33, C1[I12][ty][tx + 1],
+                                     C1[I12][ty][tx], C0[I23][ty][tx], C1[I23][ty][tx]);
+            if (MODE == 1) r += S.rv[K & 1][1][ty][tx];
+            o.V2[g] = Vin[1][ty + 1][tx + 1] + r * ((C0[IX][ty][tx + 1] + dtc) * h);
+        }
+        if (I <= n1 - 2 && J <= n2 - 2) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
+            float r = mom3<float, G>(p.geo, d1, d2, d3, I, J, C1[I33][ty + 1][tx + 1] - C1[IP][ty + 1][tx + 1], q33, C1[I13][ty][tx + 1],
+                                     C1[I13][ty][tx], C1[I23][ty + 1][tx], C1[I23][ty][tx]);
+            if (G == CART && MODE == 0) r -= p.g * (h * (p.rho[g - d.sz] + S.old[K & 1][IX][ty + 1][tx + 1]));  // plane K-1's slot is being refilled
+            if (MODE == 1) r += S.rv[K & 1][2][ty][tx];
+            o.V3[g] = Vin[2][ty + 1][tx + 1] + r * ((C1[IX][ty + 1][tx + 1] + dtc) * h);
+        }
+    };
+
+    // prologue: inputs kA-1, kA and old kA-1 (group A); inputs kA+1, old kA, rV kA (group B)
+    issue_inputs(kA - 1);
+    issue_inputs(kA);
+    issue_old(kA - 1);
+    cp_async_commit();
+    issue_inputs(kA + 1);
+    issue_old(kA);
+    issue_rv(kA);
+    cp_async_commit();
+    cp_async_wait<1>();
+    __syncthreads();
+    if (kA >= 1) stage1(kA - 1, false);
+    for (int K = kA; K < kB; ++K) {
+        __syncthreads();  // slots of plane K-1 are free
+        issue_inputs(K + 2);
+        issue_old(K + 1);
+        issue_rv(K + 1);
+        cp_async_commit();
+        cp_async_wait<1>();  // inputs K+1, old K, rV K have landed
+        __syncthreads();
+        stage1(K, true);
+        __syncthreads();
+        velocity(K);
+    }
+    cp_async_wait<0>();
+}
+
+inline size_t fused_smem_bytes() { return sizeof(FusedSmem); }
+
+}  // namespace sph

@@ -12,7 +12,7 @@
 // the template parameter G and the 1D tables in Geo.  The FP32 fused sweep in
 // sph_fused.cuh implements the same arithmetic with shared-memory tiling.
 #pragma once
-#include "sph_common.cuh"
+#include "sph_core.cuh"
 
 namespace sph {
 
@@ -46,83 +46,42 @@ __global__ void __launch_bounds__(256) k_stress(KP<T> p) {
     if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
     const int sy = d.sy, sz = d.sz;
     const int c = i + sy * j + sz * k;
-    const T h = T(0.5), q4 = T(0.25);
     {
-        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
-        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
-        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
-        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
-        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
-        T D11, D22, D33;
-        if (G != CART) {
-            const T t3 = div * T(1.0 / 3.0);
-            D11 = p.d1 * d1v - t3;
-            D22 = m.a2 * d2v + m.e1 * avx - t3;
-            D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
-        } else {
-            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
-        }
+        const CellD<T> D = cell_strain<T, G>(p.geo, p.d1, p.d2, p.d3, i, j, p.V1[c], p.V1[c + 1], p.V2[c], p.V2[c + sy], p.V3[c], p.V3[c + sz]);
         const T sm = p.etaSM[c], e = p.eta[c];
         const T gs = p.gsc * sm, kb = p.kbc * sm;
         const T f = e / (e + gs);  // 1/(1 + GSDT/η)
-        T dv = div;
+        T dv = D.div;
         if (RHS) dv += p.rP[c];
-        p.P[c] = p.P[c] - kb * dv;
-        p.t11[c] = (p.t11[c] + T(2) * gs * D11) * f;
-        p.t22[c] = (p.t22[c] + T(2) * gs * D22) * f;
-        p.t33[c] = (p.t33[c] + T(2) * gs * D33) * f;
+        T Pn = p.P[c] - kb * dv;
+        const T n22 = (p.t22[c] + T(2) * gs * D.D22) * f, n33 = (p.t33[c] + T(2) * gs * D.D33) * f;
+        if (p.traction) traction_pressure(j, k, d.n2, d.n3, n22, n33, p.sig2, p.sig3, Pn);
+        p.P[c] = Pn;
+        p.t11[c] = (p.t11[c] + T(2) * gs * D.D11) * f;
+        p.t22[c] = n22;
+        p.t33[c] = n33;
         p.DT_R[c] = p.vpdt2 / (kb + gs * f);
     }
     // τ12 at (i+1/2, j+1/2, k+1): cells (i|i+1, j|j+1, k+1)
     if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
         const int q = c + sz;
-        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sy] + p.etaSM[q + 1] + p.etaSM[q + 1 + sy]) * q4);
-        const T aE = (p.eta[q] + p.eta[q + sy] + p.eta[q + 1] + p.eta[q + 1 + sy]) * q4;
-        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1];   // V2 (i, j+1, k+1), (i+1, j+1, k+1)
-        const T v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];    // V1 (i+1, j, k+1), (i+1, j+1, k+1)
-        T D;
-        if (G != CART) {
-            const T iR = p.geo.invRh[i];
-            D = (v2b - v2a) * p.d1 + iR * (v1b - v1a) * p.d2 - (v2a + v2b) * h * iR;
-        } else {
-            D = (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
-        }
-        p.t12[c] = (p.t12[c] + aG * D) * (aE / (aE + aG));
+        const T D = edge12<T, G>(p.geo, p.d1, p.d2, i, p.V2[q + sy], p.V2[q + sy + 1], p.V1[q + 1], p.V1[q + 1 + sy]);
+        p.t12[c] = edge_update(p.t12[c], p.gsc, p.etaSM[q] + p.etaSM[q + sy] + p.etaSM[q + 1] + p.etaSM[q + 1 + sy],
+                               p.eta[q] + p.eta[q + sy] + p.eta[q + 1] + p.eta[q + 1 + sy], D);
     }
     // τ13 at (i+1/2, j+1, k+1/2): cells (i|i+1, j+1, k|k+1)
     if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
         const int q = c + sy;
-        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + 1] + p.etaSM[q + 1 + sz]) * q4);
-        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + 1] + p.eta[q + 1 + sz]) * q4;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1];   // V3 (i, j+1, k+1), (i+1, j+1, k+1)
-        const T v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];    // V1 (i+1, j+1, k), (i+1, j+1, k+1)
-        T D;
-        if (G == SPH) {
-            const T iR = p.geo.invRh[i];
-            D = (v3b - v3a) * p.d1 + iR * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * iR;
-        } else {
-            D = (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
-        }
-        p.t13[c] = (p.t13[c] + aG * D) * (aE / (aE + aG));
+        const T D = edge13<T, G>(p.geo, p.d1, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + 1], p.V1[q + 1], p.V1[q + 1 + sz]);
+        p.t13[c] = edge_update(p.t13[c], p.gsc, p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + 1] + p.etaSM[q + 1 + sz],
+                               p.eta[q] + p.eta[q + sz] + p.eta[q + 1] + p.eta[q + 1 + sz], D);
     }
     // τ23 at (i+1, j+1/2, k+1/2): cells (i+1, j|j+1, k|k+1)
     if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
         const int q = c + 1;
-        const T aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + sy] + p.etaSM[q + sy + sz]) * q4);
-        const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + sy] + p.eta[q + sy + sz]) * q4;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy];  // V3 (i+1, j, k+1), (i+1, j+1, k+1)
-        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];  // V2 (i+1, j+1, k), (i+1, j+1, k+1)
-        T D;
-        if (G == SPH) {
-            const T iR = p.geo.invRc[i + 1];
-            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
-        } else if (G == CYL) {
-            const T iR = p.geo.invRc[i + 1];
-            D = iR * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        } else {
-            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        }
-        p.t23[c] = (p.t23[c] + aG * D) * (aE / (aE + aG));
+        const T D = edge23<T, G>(p.geo, p.d2, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + sy], p.V2[q + sy], p.V2[q + sy + sz]);
+        p.t23[c] = edge_update(p.t23[c], p.gsc, p.etaSM[q] + p.etaSM[q + sz] + p.etaSM[q + sy] + p.etaSM[q + sy + sz],
+                               p.eta[q] + p.eta[q + sz] + p.eta[q + sy] + p.eta[q + sy + sz], D);
     }
 }
 
@@ -180,47 +139,21 @@ __global__ void __launch_bounds__(256) k_strain(KP<T> p) {
     if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
     const int sy = d.sy, sz = d.sz;
     const int c = i + sy * j + sz * k;
-    const T h = T(0.5);
     {
-        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
-        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
-        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
-        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
-        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
-        T D11, D22, D33;
-        if (G != CART) {
-            const T t3 = div * T(1.0 / 3.0);
-            D11 = p.d1 * d1v - t3; D22 = m.a2 * d2v + m.e1 * avx - t3; D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
-        } else {
-            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
-        }
-        p.sDD[c] = h * (D11 * D11 + D22 * D22 + D33 * D33);
+        const CellD<T> D = cell_strain<T, G>(p.geo, p.d1, p.d2, p.d3, i, j, p.V1[c], p.V1[c + 1], p.V2[c], p.V2[c + sy], p.V3[c], p.V3[c + sz]);
+        p.sDD[c] = T(0.5) * (D.D11 * D.D11 + D.D22 * D.D22 + D.D33 * D.D33);
     }
     if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
         const int q = c + sz;
-        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];
-        p.s12[c] = (G != CART) ? (v2b - v2a) * p.d1 + p.geo.invRh[i] * (v1b - v1a) * p.d2 - (v2a + v2b) * h * p.geo.invRh[i]
-                               : (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
+        p.s12[c] = edge12<T, G>(p.geo, p.d1, p.d2, i, p.V2[q + sy], p.V2[q + sy + 1], p.V1[q + 1], p.V1[q + 1 + sy]);
     }
     if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
         const int q = c + sy;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];
-        p.s13[c] = (G == SPH) ? (v3b - v3a) * p.d1 + p.geo.invRh[i] * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * p.geo.invRh[i]
-                              : (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
+        p.s13[c] = edge13<T, G>(p.geo, p.d1, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + 1], p.V1[q + 1], p.V1[q + 1 + sz]);
     }
     if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
         const int q = c + 1;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy], v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];
-        T D;
-        if (G == SPH) {
-            const T iR = p.geo.invRc[i + 1];
-            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
-        } else if (G == CYL) {
-            D = p.geo.invRc[i + 1] * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        } else {
-            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        }
-        p.s23[c] = D;
+        p.s23[c] = edge23<T, G>(p.geo, p.d2, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + sy], p.V2[q + sy], p.V2[q + sy + sz]);
     }
 }
 
@@ -267,66 +200,27 @@ __device__ __forceinline__ void momentum(const KP<T>& p, int I, int J, int K, T 
     ok[0] = (J <= d.n2 - 2 && K <= d.n3 - 2);
     ok[1] = (I <= d.n1 - 2 && K <= d.n3 - 2);
     ok[2] = (I <= d.n1 - 2 && J <= d.n2 - 2);
-    // V1 (I-1/2, J, K)
-    if (ok[0]) {
+    if (ok[0]) {  // V1 (I-1/2, J, K)
         const int m = c - 1;
         const T Pm = p.P[m];
-        const T s11m = p.t11[m] - Pm, s22m = p.t22[m] - Pm, s33m = p.t33[m] - Pm;
-        const T ta = p.t12[m - sz], tb = p.t12[m - sy - sz];       // τ12 (I-1, J, K-1), (I-1, J-1, K-1)
-        const T ua = p.t13[m - sy], ub = p.t13[m - sy - sz];       // τ13 (I-1, J-1, K), (I-1, J-1, K-1)
-        T r;
-        if (G == SPH) {
-            const T iR = p.geo.invRh[I - 1], iS = p.geo.invSinC[J], ct = p.geo.cotC[J];
-            r = (s11 - s11m) * p.d1 + iR * (ta - tb) * p.d2 + iR * iS * (ua - ub) * p.d3 +
-                (T(2) * ((s11m + s11) * h) - (((s22m + s22) * h) + ((s33m + s33) * h))) * iR + ((tb + ta) * h) * iR * ct;
-        } else if (G == CYL) {
-            const T iR = p.geo.invRh[I - 1];
-            r = (s11 - s11m) * p.d1 + iR * (ta - tb) * p.d2 + (ua - ub) * p.d3 + (((s11m + s11) * h) - ((s22m + s22) * h)) * iR;
-        } else {
-            r = (s11 - s11m) * p.d1 + (ta - tb) * p.d2 + (ua - ub) * p.d3;
-        }
+        T r = mom1<T, G>(p.geo, p.d1, p.d2, p.d3, I, J, p.t11[m] - Pm, s11, p.t22[m] - Pm, s22, p.t33[m] - Pm, s33,
+                         p.t12[m - sz], p.t12[m - sy - sz], p.t13[m - sy], p.t13[m - sy - sz]);
         if (G != CART && GRAV) r -= (p.rho[m] * p.g + p.rho[c] * p.g) * h;
         if (RHS) r += p.rV1[c];
         dv[0] = r;
     }
-    // V2 (I, J-1/2, K)
-    if (ok[1]) {
+    if (ok[1]) {  // V2 (I, J-1/2, K)
         const int m = c - sy;
         const T Pm = p.P[m];
-        const T s22m = p.t22[m] - Pm, s33m = p.t33[m] - Pm;
-        const T ta = p.t12[c - sy - sz], tb = p.t12[c - 1 - sy - sz];  // τ12 (I, J-1, K-1), (I-1, J-1, K-1)
-        const T ua = p.t23[c - 1 - sy], ub = p.t23[c - 1 - sy - sz];   // τ23 (I-1, J-1, K), (I-1, J-1, K-1)
-        T r;
-        if (G == SPH) {
-            const T iR = p.geo.invRc[I], iS = p.geo.invSinH[J - 1], ct = p.geo.cotH[J - 1];
-            r = (ta - tb) * p.d1 + iR * (s22 - s22m) * p.d2 + iR * iS * (ua - ub) * p.d3 + T(3) * ((tb + ta) * h) * iR +
-                (((s22m + s22) * h) - ((s33m + s33) * h)) * iR * ct;
-        } else if (G == CYL) {
-            const T iR = p.geo.invRc[I];
-            r = (ta - tb) * p.d1 + iR * (s22 - s22m) * p.d2 + (ua - ub) * p.d3 + T(2) * ((tb + ta) * h) * iR;
-        } else {
-            r = (ta - tb) * p.d1 + (s22 - s22m) * p.d2 + (ua - ub) * p.d3;
-        }
+        T r = mom2<T, G>(p.geo, p.d1, p.d2, p.d3, I, J, p.t22[m] - Pm, s22, p.t33[m] - Pm, s33,
+                         p.t12[c - sy - sz], p.t12[c - 1 - sy - sz], p.t23[c - 1 - sy], p.t23[c - 1 - sy - sz]);
         if (RHS) r += p.rV2[c];
         dv[1] = r;
     }
-    // V3 (I, J, K-1/2)
-    if (ok[2]) {
+    if (ok[2]) {  // V3 (I, J, K-1/2)
         const int m = c - sz;
-        const T s33m = p.t33[m] - p.P[m];
-        const T ta = p.t13[c - sy - sz], tb = p.t13[c - 1 - sy - sz];  // τ13 (I, J-1, K-1), (I-1, J-1, K-1)
-        const T ua = p.t23[c - 1 - sz], ub = p.t23[c - 1 - sy - sz];   // τ23 (I-1, J, K-1), (I-1, J-1, K-1)
-        T r;
-        if (G == SPH) {
-            const T iR = p.geo.invRc[I], iS = p.geo.invSinC[J], ct = p.geo.cotC[J];
-            r = (ta - tb) * p.d1 + iR * (ua - ub) * p.d2 + iR * iS * (s33 - s33m) * p.d3 + T(3) * ((tb + ta) * h) * iR +
-                T(2) * ((ub + ua) * h) * iR * ct;
-        } else if (G == CYL) {
-            const T iR = p.geo.invRc[I];
-            r = (ta - tb) * p.d1 + iR * (ua - ub) * p.d2 + (s33 - s33m) * p.d3 + ((tb + ta) * h) * iR;
-        } else {
-            r = (ta - tb) * p.d1 + (ua - ub) * p.d2 + (s33 - s33m) * p.d3;
-        }
+        T r = mom3<T, G>(p.geo, p.d1, p.d2, p.d3, I, J, p.t33[m] - p.P[m], s33, p.t13[c - sy - sz], p.t13[c - 1 - sy - sz],
+                         p.t23[c - 1 - sz], p.t23[c - 1 - sy - sz]);
         if (G == CART && GRAV) r -= p.g * (h * (p.rho[m] + p.rho[c]));
         if (RHS) r += p.rV3[c];
         dv[2] = r;
@@ -398,54 +292,27 @@ __global__ void __launch_bounds__(256) k_tau_visc(KP<T> p) {
     if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
     const int sy = d.sy, sz = d.sz;
     const int c = i + sy * j + sz * k;
-    const T h = T(0.5), q4 = T(0.25);
+    const T q4 = T(0.25);
     {
-        const CellMetric<T> m = cell_metric<T, G>(p, i, j);
-        const T v1m = p.V1[c], v1p = p.V1[c + 1], v2m = p.V2[c], v2p = p.V2[c + sy], v3m = p.V3[c], v3p = p.V3[c + sz];
-        const T d1v = v1p - v1m, d2v = v2p - v2m, d3v = v3p - v3m;
-        const T avx = (v1m + v1p) * h, avy = (v2m + v2p) * h;
-        const T div = p.d1 * d1v + m.a2 * d2v + m.a3 * d3v + m.c1 * avx + m.c2 * avy;
-        T D11, D22, D33;
-        if (G != CART) {
-            const T t3 = div * T(1.0 / 3.0);
-            D11 = p.d1 * d1v - t3; D22 = m.a2 * d2v + m.e1 * avx - t3; D33 = m.a3 * d3v + m.e1b * avx + m.e2 * avy - t3;
-        } else {
-            D11 = p.d1 * d1v; D22 = m.a2 * d2v; D33 = m.a3 * d3v;
-        }
+        const CellD<T> D = cell_strain<T, G>(p.geo, p.d1, p.d2, p.d3, i, j, p.V1[c], p.V1[c + 1], p.V2[c], p.V2[c + sy], p.V3[c], p.V3[c + sz]);
         const T e2 = T(2) * p.eta[c];
-        p.t11[c] = e2 * D11; p.t22[c] = e2 * D22; p.t33[c] = e2 * D33;
-        p.rP[c] = div;
+        p.t11[c] = e2 * D.D11; p.t22[c] = e2 * D.D22; p.t33[c] = e2 * D.D33;
+        p.rP[c] = D.div;
     }
     if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
         const int q = c + sz;
         const T aE = (p.eta[q] + p.eta[q + sy] + p.eta[q + 1] + p.eta[q + 1 + sy]) * q4;
-        const T v2a = p.V2[q + sy], v2b = p.V2[q + sy + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sy];
-        const T D = (G != CART) ? (v2b - v2a) * p.d1 + p.geo.invRh[i] * (v1b - v1a) * p.d2 - (v2a + v2b) * h * p.geo.invRh[i]
-                                : (v1b - v1a) * p.d2 + (v2b - v2a) * p.d1;
-        p.t12[c] = aE * D;
+        p.t12[c] = aE * edge12<T, G>(p.geo, p.d1, p.d2, i, p.V2[q + sy], p.V2[q + sy + 1], p.V1[q + 1], p.V1[q + 1 + sy]);
     }
     if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
         const int q = c + sy;
         const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + 1] + p.eta[q + 1 + sz]) * q4;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + 1], v1a = p.V1[q + 1], v1b = p.V1[q + 1 + sz];
-        const T D = (G == SPH) ? (v3b - v3a) * p.d1 + p.geo.invRh[i] * p.geo.invSinC[j + 1] * (v1b - v1a) * p.d3 - (v3a + v3b) * h * p.geo.invRh[i]
-                               : (v3b - v3a) * p.d1 + (v1b - v1a) * p.d3;
-        p.t13[c] = aE * D;
+        p.t13[c] = aE * edge13<T, G>(p.geo, p.d1, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + 1], p.V1[q + 1], p.V1[q + 1 + sz]);
     }
     if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
         const int q = c + 1;
         const T aE = (p.eta[q] + p.eta[q + sz] + p.eta[q + sy] + p.eta[q + sy + sz]) * q4;
-        const T v3a = p.V3[q + sz], v3b = p.V3[q + sz + sy], v2a = p.V2[q + sy], v2b = p.V2[q + sy + sz];
-        T D;
-        if (G == SPH) {
-            const T iR = p.geo.invRc[i + 1];
-            D = iR * (v3b - v3a) * p.d2 + iR * p.geo.invSinH[j] * (v2b - v2a) * p.d3 - (v3a + v3b) * h * iR * p.geo.cotH[j];
-        } else if (G == CYL) {
-            D = p.geo.invRc[i + 1] * (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        } else {
-            D = (v3b - v3a) * p.d2 + (v2b - v2a) * p.d3;
-        }
-        p.t23[c] = aE * D;
+        p.t23[c] = aE * edge23<T, G>(p.geo, p.d2, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + sy], p.V2[q + sy], p.V2[q + sy + sz]);
     }
 }
 
@@ -506,37 +373,45 @@ __global__ void k_bc(KP<T> p, BcStage st, int homog) {
                     val = T(2) * (xc[idx] - T(op.c1)) * T(op.c0) - A[ci];
                     break;
                 }
-                default: {  // BC_STRESS on V2 (D == 1) or V3 (D == 2)
+                default: {  // BC_STRESS: normal ghost of V2 (D == 1) or V3 (D == 2) from div V = 0 in the boundary cell
                     const int cellb = side == 0 ? 0 : ext[D] - 2;        // boundary cell index along D
                     const int cc = base + cellb * stride[D];             // boundary cell
                     const int i = (D == 0) ? cellb : u;
                     const int j = (D == 1) ? cellb : (du == 1 ? u : v);
                     const CellMetric<T> m = cell_metric<T, G>(p, i, j);
-                    const T sig = homog ? T(0) : (D == 1 ? p.sig2 : p.sig3);
                     const T sgn = side == 0 ? T(-1) : T(1);
                     const T avx = (p.V1[cc] + p.V1[cc + 1]) * T(0.5);
                     const T vin = A[ci];
-                    const T Dt = (sig + p.P[cc]) / (T(2) * p.eta[cc]);
-                    T A0, B, C0, Cg;
+                    T A0, B;
                     if (D == 1) {
                         A0 = p.d1 * (p.V1[cc + 1] - p.V1[cc]) + m.a3 * (p.V3[cc + sz] - p.V3[cc]) + m.c1 * avx + m.a2 * (-sgn) * vin + m.c2 * T(0.5) * vin;
                         B = m.a2 * sgn + T(0.5) * m.c2;
-                        C0 = m.a2 * (-sgn) * vin + m.e1 * avx - A0 / T(3);
-                        Cg = m.a2 * sgn - B / T(3);
                     } else {
                         const T avy = (p.V2[cc] + p.V2[cc + sy]) * T(0.5);
                         A0 = p.d1 * (p.V1[cc + 1] - p.V1[cc]) + m.a2 * (p.V2[cc + sy] - p.V2[cc]) + m.c1 * avx + m.c2 * avy + m.a3 * (-sgn) * vin;
                         B = m.a3 * sgn;
-                        C0 = m.a3 * (-sgn) * vin + m.e1b * avx + m.e2 * avy - A0 / T(3);
-                        Cg = m.a3 * sgn - B / T(3);
                     }
-                    val = (Dt - C0) / Cg;
+                    val = -A0 / B;
                     break;
                 }
             }
             A[cb] = val;
         }
     }
+}
+
+// ---------------------------------------------------------------------------
+// P_out = P except on the boundary cells of the normal-stress BC, where
+// P_out = τ_nn - σ_bc from the given stresses (residual evaluation)
+template <typename T>
+__global__ void k_traction_pressure(KP<T> p, T* __restrict__ Pout) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int c = i + d.sy * j + d.sz * k;
+    T P = p.P[c];
+    traction_pressure(j, k, d.n2, d.n3, p.t22[c], p.t33[c], p.sig2, p.sig3, P);
+    Pout[c] = P;
 }
 
 // ---------------------------------------------------------------------------

@@ -10,12 +10,14 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <string>
 #include <vector>
 
 #include "sph_pt.cuh"
+#include "sph_fused.cuh"
 #include "sphstokes.h"
 
 using namespace sph;
@@ -44,6 +46,9 @@ enum FieldSlot {
     F_ETA, F_ETA_INI, F_ETA_SM, F_DT_R, F_TII, F_RHO, F_ETA_PL, F_ETA_OUT,
     F_V1E, F_V2E, F_V3E, F_RP, F_RV1, F_RV2, F_RV3, F_SDD, F_S12, F_S13, F_S23,
     F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23,
+    // second copy of the PT state (ping-pong of the fused sweep)
+    F_A_P, F_A_V1, F_A_V2, F_A_V3, F_A_T11, F_A_T22, F_A_T33, F_A_T12, F_A_T13, F_A_T23,
+    F_PRES,  // pressure of the residual evaluation (traction-slaved boundary cells)
     F_NSLOTS
 };
 
@@ -72,8 +77,18 @@ struct Ctx {
     double cur_n = 1.0;
     double f_scale = 1.0;
     double last_ms = 0.0;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr, ev4 = nullptr;
+    double sweep_ms = 0.0, outer_ms = 0.0;  // device time split of the last solve (MIXED)
     std::vector<double> hx1, hx2, hx3;  // node coordinates (host)
+    bool corr_ready = false;  // a correction problem is prepared in the FP32 state (MIXED)
+    double corr_r0 = 0.0;     // max|r_V| of the prepared correction problem
+    // CUDA graphs of `graph_len` correction sweeps, one per ping-pong arrangement
+    cudaGraphExec_t corr_graph[2] = {nullptr, nullptr};
+    float* corr_graph_key[2] = {nullptr, nullptr};   // F_P pointer at capture time
+    int graph_len = 0;
+    bool use_graphs = true;
+    bool fused = true;   // FP32 sweeps use the fused kernel
+    int fused_chunk = 0; // planes per block of the fused sweep
 };
 
 constexpr int kRedSlots = 16;
@@ -137,6 +152,7 @@ KP<T> make_kp(Ctx& c, State<T>& s) {
     p.g = T(q.g);
     p.tau_C = T(q.tau_C); p.n_exp = T(c.cur_n); p.relax = T(q.relax); p.edot_bg = T(q.edot_bg);
     p.sig2 = T(q.sig_bc[1]); p.sig3 = T(q.sig_bc[2]);
+    p.traction = q.bc == SPH_BC_STRESS ? 1 : 0;
     p.red = c.red;
     return p;
 }
@@ -361,9 +377,21 @@ int sync64(Ctx& c) {
 
 // ---------------------------------------------------------------------------
 // one reference PT iteration on state s
+// ηSM: `etasm_passes` applications of the 7-point max filter (maxloc! + copy_BC!);
+// intermediate passes go through the η_out scratch field, the last one into ηSM
 template <typename T, int G>
 void launch_maxloc(Ctx& c, KP<T>& p) {
-    k_maxloc<T><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p, G == CART);
+    const int passes = c.prm.etasm_passes > 1 ? c.prm.etasm_passes : 1;
+    KP<T> q = p;
+    T* src = p.eta;
+    for (int i = 0; i < passes; ++i) {
+        const bool last = i == passes - 1;
+        T* dst = last ? p.etaSM : (((passes - 1 - i) & 1) ? p.eta_out : p.etaSM);
+        q.eta = src;
+        q.etaSM = dst;
+        k_maxloc<T><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(q, G == CART);
+        src = dst;
+    }
 }
 
 template <typename T, int G>
@@ -392,12 +420,86 @@ void iterate_one(Ctx& c, State<T>& s) {
     launch_bc<T, G>(c, p, 0);
 }
 
+// the fused FP32 sweep: new state into the second buffer set, then swap sets
+void swap_state(State<float>& s) {
+    const int a[10] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
+    const int b[10] = {F_A_P, F_A_V1, F_A_V2, F_A_V3, F_A_T11, F_A_T22, F_A_T33, F_A_T12, F_A_T13, F_A_T23};
+    for (int i = 0; i < 10; ++i) std::swap(s.f[a[i]], s.f[b[i]]);
+}
+
+int fused_chunk(const Ctx& c) {
+    if (c.fused_chunk > 0) return c.fused_chunk;
+    const long long xy = (long long)((c.d.n1 + FTX - 1) / FTX) * ((c.d.n2 + FTY - 1) / FTY);
+    long long nch = (152LL * 3 + xy - 1) / xy;  // about three resident blocks per SM (one wave)
+    if (nch < 1) nch = 1;
+    int k = (int)((c.d.n3 + nch - 1) / nch);
+    return k < 4 ? 4 : k;
+}
+
+template <int G, int MODE>
+void set_fused_attr() {
+    cudaFuncSetAttribute(k_fused<G, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem_bytes());
+}
+int set_fused_attrs() {
+    set_fused_attr<SPH, 0>(); set_fused_attr<SPH, 1>();
+    set_fused_attr<CYL, 0>(); set_fused_attr<CYL, 1>();
+    set_fused_attr<CART, 0>(); set_fused_attr<CART, 1>();
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+template <int G, int MODE>
+void launch_fused(Ctx& c, KP<float>& p, State<float>& s) {
+    FusedOut<float> o;
+    o.P = s.f[F_A_P]; o.V1 = s.f[F_A_V1]; o.V2 = s.f[F_A_V2]; o.V3 = s.f[F_A_V3];
+    o.t11 = s.f[F_A_T11]; o.t22 = s.f[F_A_T22]; o.t33 = s.f[F_A_T33]; o.t12 = s.f[F_A_T12]; o.t13 = s.f[F_A_T13]; o.t23 = s.f[F_A_T23];
+    const int kc = fused_chunk(c);
+    dim3 grid((c.d.n1 + FTX - 1) / FTX, (c.d.n2 + FTY - 1) / FTY, (c.d.n3 + kc - 1) / kc);
+    k_fused<G, MODE><<<grid, dim3(FNT, 1, 1), fused_smem_bytes(), c.stream>>>(p, o, kc);
+}
+
+// one reference iteration with the fused sweep (FP32)
+template <int G>
+void iterate_fused(Ctx& c, State<float>& s) {
+    KP<float> p = make_kp<float>(c, s);
+    launch_maxloc<float, G>(c, p);
+    launch_fused<G, 0>(c, p, s);
+    swap_state(s);
+    KP<float> q = make_kp<float>(c, s);
+    if (c.prm.rheology == SPH_RHEO_EDOT_POWER_RELAX) {
+        // the law uses the velocities the stress update used (the previous set)
+        KP<float> r = q;
+        r.V1 = s.f[F_A_V1]; r.V2 = s.f[F_A_V2]; r.V3 = s.f[F_A_V3];
+        launch_rheology<float, G>(c, s, r);
+        q.eta = s.f[F_ETA]; q.eta_out = s.f[F_ETA_OUT];
+    } else {
+        launch_rheology<float, G>(c, s, q);
+    }
+    launch_bc<float, G>(c, q, 0);
+}
+
 template <typename T>
 void iterate_dispatch(Ctx& c, State<T>& s) {
     switch (c.prm.geometry) {
         case SPH_GEOM_SPHERICAL: iterate_one<T, SPH>(c, s); break;
         case SPH_GEOM_CYLINDRICAL: iterate_one<T, CYL>(c, s); break;
         default: iterate_one<T, CART>(c, s); break;
+    }
+}
+template <>
+void iterate_dispatch<float>(Ctx& c, State<float>& s) {
+    if (c.fused) {
+        switch (c.prm.geometry) {
+            case SPH_GEOM_SPHERICAL: iterate_fused<SPH>(c, s); break;
+            case SPH_GEOM_CYLINDRICAL: iterate_fused<CYL>(c, s); break;
+            default: iterate_fused<CART>(c, s); break;
+        }
+        return;
+    }
+    switch (c.prm.geometry) {
+        case SPH_GEOM_SPHERICAL: iterate_one<float, SPH>(c, s); break;
+        case SPH_GEOM_CYLINDRICAL: iterate_one<float, CYL>(c, s); break;
+        default: iterate_one<float, CART>(c, s); break;
     }
 }
 
@@ -467,6 +569,10 @@ int residual64_g(Ctx& c, double out[7], bool eta_from_law) {
     r.eta = const_cast<double*>(eta_eff);
     r.t11 = s.f[F_Q11]; r.t22 = s.f[F_Q22]; r.t33 = s.f[F_Q33]; r.t12 = s.f[F_Q12]; r.t13 = s.f[F_Q13]; r.t23 = s.f[F_Q23];
     k_tau_visc<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(r);
+    if (r.traction) {
+        k_traction_pressure<double><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(r, s.f[F_PRES]);
+        r.P = s.f[F_PRES];
+    }
     k_velocity<double, G, 2><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(r);
     CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
     launch_maxabs<double>(c, s.f[F_RV1], nullptr, 0);
@@ -558,6 +664,122 @@ int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_sol
 //   inner: PT on (δV, δP, δτ) with η frozen at η_eff, homogeneous BCs,
 //          δP -= KBDT (div δV + r_P), δV += DT_R (div(-δP + δτ) + r_V)
 //   V += δV, P += δP (FP64)
+// FP64 viscosity η_eff(V), the full BC program and the residual of the FP64 state
+template <int G>
+int outer_residual(Ctx& c, double out[7]) {
+    State<double>& s = c.s64;
+    KP<double> p = make_kp<double>(c, s);
+    const long long vol = c.d.vol;
+    if (c.prm.rheology == SPH_RHEO_EDOT_POWER_RELAX) {
+        k_strain<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        k_edot_law<double, false><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
+        CK(cudaMemcpyAsync(s.f[F_ETA], s.f[F_ETA_OUT], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
+    }
+    launch_bc<double, G>(c, p, 0);
+    return residual64_g<G>(c, out, false);
+}
+
+// freeze η_eff, ηSM and the FP64 residual into the FP32 correction problem, zero δ
+template <int G>
+int prepare_correction(Ctx& c, const double out[7]) {
+    State<double>& s = c.s64;
+    State<float>& t = c.s32;
+    const long long vol = c.d.vol;
+    k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_ETA], s.f[F_ETA], vol);
+    k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV1], s.f[F_RV1], vol);
+    k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV2], s.f[F_RV2], vol);
+    k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV3], s.f[F_RV3], vol);
+    k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RP], s.f[F_RP], vol);
+    const int zero[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23,
+                        F_A_P, F_A_V1, F_A_V2, F_A_V3, F_A_T11, F_A_T22, F_A_T33, F_A_T12, F_A_T13, F_A_T23};
+    for (int z : zero) CK(cudaMemsetAsync(t.f[z], 0, sizeof(float) * vol, c.stream));
+    KP<float> q = make_kp<float>(c, t);
+    launch_maxloc<float, G>(c, q);
+    CK(cudaGetLastError());
+    c.corr_r0 = std::max(out[0], std::max(out[1], out[2]));
+    c.corr_ready = true;
+    c.stale32 = true;  // the FP32 state no longer mirrors the FP64 state
+    return SPH_OK;
+}
+
+// KP of the correction problem: homogeneous boundary data
+KP<float> make_kp_corr(Ctx& c) {
+    KP<float> q = make_kp<float>(c, c.s32);
+    q.sig2 = 0.f;
+    q.sig3 = 0.f;
+    return q;
+}
+
+// one FP32 sweep of the correction problem (fused or one kernel per step) + homogeneous BCs
+template <int G>
+void correction_sweep(Ctx& c) {
+    State<float>& t = c.s32;
+    KP<float> q = make_kp_corr(c);
+    if (c.fused) {
+        launch_fused<G, 1>(c, q, t);
+        swap_state(t);
+        q = make_kp_corr(c);
+    } else {
+        k_stress<float, G, true><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(q);
+        k_velocity<float, G, 1><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
+    }
+    launch_bc<float, G>(c, q, 1);
+}
+
+// run `n` correction sweeps; with graphs enabled and n even, replays a captured
+// graph of n sweeps (after an even count the ping-pong arrangement of the
+// buffers is back where it started, so the graph stays valid)
+template <int G>
+int run_correction_sweeps(Ctx& c, int n) {
+    if (n <= 0) return SPH_OK;
+    if (!c.use_graphs || (n & 1) || n < 8) {
+        for (int i = 0; i < n; ++i) correction_sweep<G>(c);
+        CK(cudaGetLastError());
+        return SPH_OK;
+    }
+    if (n != c.graph_len) {
+        for (int i = 0; i < 2; ++i) {
+            if (c.corr_graph[i]) cudaGraphExecDestroy(c.corr_graph[i]);
+            c.corr_graph[i] = nullptr;
+            c.corr_graph_key[i] = nullptr;
+        }
+        c.graph_len = n;
+    }
+    float* key = c.s32.f[F_P];
+    int slot = -1;
+    for (int i = 0; i < 2; ++i)
+        if (c.corr_graph[i] && c.corr_graph_key[i] == key) slot = i;
+    if (slot < 0) {
+        slot = c.corr_graph[0] ? 1 : 0;
+        if (c.corr_graph[slot]) { cudaGraphExecDestroy(c.corr_graph[slot]); c.corr_graph[slot] = nullptr; }
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < n; ++i) correction_sweep<G>(c);  // recorded, not run
+        cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c.corr_graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        c.corr_graph_key[slot] = key;
+    }
+    CK(cudaGraphLaunch(c.corr_graph[slot], c.stream));
+    return SPH_OK;
+}
+
+// V += δV, P += δP (FP64)
+int apply_correction(Ctx& c) {
+    State<double>& s = c.s64;
+    State<float>& t = c.s32;
+    const long long vol = c.d.vol;
+    k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
+    k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
+    k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
+    k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
+    CK(cudaGetLastError());
+    c.corr_ready = false;
+    return SPH_OK;
+}
+
 template <int G>
 int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t* hi, double* he, int64_t cap) {
     State<double>& s = c.s64;
@@ -594,17 +816,11 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
         if (!law) k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_ETA], t.f[F_ETA], vol);
         CK(cudaGetLastError());
     }
-    KP<double> p = make_kp<double>(c, s);
+    float ms = 0.f;
     for (int outer = 0; outer <= o.max_outer; ++outer) {
-        // η_eff(V) in FP64, then the full BC program (stress ghosts use η_eff)
-        if (law) {
-            k_strain<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
-            k_edot_law<double, false><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(p);
-            CK(cudaMemcpyAsync(s.f[F_ETA], s.f[F_ETA_OUT], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
-        }
-        launch_bc<double, G>(c, p, 0);
         double out[7];
-        int rc = residual64_g<G>(c, out, false);
+        CK(cudaEventRecord(c.ev2, c.stream));
+        int rc = outer_residual<G>(c, out);
         if (rc) return rc;
         err = out[6];
         if (info) {
@@ -619,42 +835,40 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
         if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
         if (err < o.tol) { status = SPH_OK; break; }
         if (outer == o.max_outer || iters >= o.maxiter) break;
-        // frozen coefficients and right-hand sides of the correction problem
-        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_ETA], s.f[F_ETA], vol);
-        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV1], s.f[F_RV1], vol);
-        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV2], s.f[F_RV2], vol);
-        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RV3], s.f[F_RV3], vol);
-        k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(t.f[F_RP], s.f[F_RP], vol);
-        const int zero[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
-        for (int z : zero) CK(cudaMemsetAsync(t.f[z], 0, sizeof(float) * vol, c.stream));
-        KP<float> q = make_kp<float>(c, t);
-        launch_maxloc<float, G>(c, q);
-        const double r0 = std::max(out[0], std::max(out[1], out[2]));
+        rc = prepare_correction<G>(c, out);
+        if (rc) return rc;
+        CK(cudaEventRecord(c.ev3, c.stream));
         const int inner_max = o.inner_max > 0 ? o.inner_max : 100000;
         int inner = 0;
         while (inner < inner_max && iters < o.maxiter) {
-            ++inner; ++iters;
-            k_stress<float, G, true><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(q);
-            k_velocity<float, G, 1><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
-            launch_bc<float, G>(c, q, 1);
-            if (inner % nout) continue;
+            const int chunk = (int)std::min<int64_t>(std::min<int64_t>(nout, inner_max - inner), o.maxiter - iters);
+            rc = run_correction_sweeps<G>(c, chunk);
+            if (rc) return rc;
+            inner += chunk; iters += chunk;
+            if (chunk < nout) break;
             // momentum residual of the correction problem with the current δ state
+            KP<float> q = make_kp_corr(c);
             CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
             k_velocity_norm<float, G><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
             CK(cudaGetLastError());
             rc = fetch_red(c);
             if (rc) return rc;
             const double ri = slot_val(c, 0);
-            if (!(ri == ri)) return fail(SPH_ERR_DIVERGED, "NaN in the FP32 correction sweeps");
-            if (ri <= o.inner_rtol * r0) break;
+            if (!(ri == ri) || std::isinf(ri)) { status = SPH_ERR_DIVERGED; break; }
+            if (ri <= o.inner_rtol * c.corr_r0) break;
         }
-        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
-        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
-        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
-        k_add_widen<float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
-        CK(cudaGetLastError());
+        CK(cudaEventRecord(c.ev4, c.stream));
+        if (status == SPH_ERR_DIVERGED) break;
+        rc = apply_correction(c);
+        if (rc) return rc;
+        CK(cudaEventSynchronize(c.ev4));
+        CK(cudaEventElapsedTime(&ms, c.ev3, c.ev4));
+        c.sweep_ms += ms;
+        CK(cudaEventElapsedTime(&ms, c.ev2, c.ev3));
+        c.outer_ms += ms;
     }
-    // final τ = 2 η_eff D(V) of the FP64 state as the stress output
+    // final τ = 2 η_eff D(V) of the FP64 state as the stress output (and the traction pressure)
+    if (c.prm.bc == SPH_BC_STRESS) CK(cudaMemcpyAsync(s.f[F_P], s.f[F_PRES], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
     {
         const int q[6] = {F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23};
         const int d[6] = {F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
@@ -741,6 +955,7 @@ int sph_params_default(sph_params* p, int32_t geometry) {
         default: return fail(SPH_ERR_INVALID, "geometry");
     }
     p->vpdt = 0.0;  // 0: dx1 * CFL with CFL = 1/(2 + 4.5 log10(vr)), set at sph_create
+    p->etasm_passes = 1;
     return SPH_OK;
 }
 
@@ -767,6 +982,8 @@ int sph_create(const sph_params* prm, void** out) {
     sph_params& q = c->prm;
     if (q.vpdt <= 0.0) q.vpdt = q.l1 / (q.n1 - 1) * (1.0 / (2.0 + 4.5 * std::log10(q.vr)));
     c->cur_n = q.n_exp;
+    c->fused = q.kernels != SPH_KERNELS_SIMPLE;
+    if (const char* e = std::getenv("SPH_FUSED_CHUNK")) c->fused_chunk = std::atoi(e);
     Dims& d = c->d;
     d.n1 = q.n1; d.n2 = q.n2; d.n3 = q.n3;
     d.px = ((q.n1 + 1 + 31) / 32) * 32; d.py = q.n2 + 1; d.pz = q.n3 + 1;
@@ -778,7 +995,9 @@ int sph_create(const sph_params* prm, void** out) {
     auto cleanup = [&](int code) { sph_destroy(c); return code; };
     if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess) return cleanup(fail(SPH_ERR_CUDA, "stream create"));
     c->stream = c->own_stream;
-    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return cleanup(fail(SPH_ERR_CUDA, "event create"));
+    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess || cudaEventCreate(&c->ev2) != cudaSuccess ||
+        cudaEventCreate(&c->ev3) != cudaSuccess || cudaEventCreate(&c->ev4) != cudaSuccess)
+        return cleanup(fail(SPH_ERR_CUDA, "event create"));
     if (cudaMalloc((void**)&c->red, sizeof(unsigned long long) * kRedSlots) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "reduction slots"));
     if (cudaMallocHost((void**)&c->hred, sizeof(unsigned long long) * kRedSlots) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "pinned slots"));
     if (cudaMalloc((void**)&c->phase, d.vol) != cudaSuccess) return cleanup(fail(SPH_ERR_NOMEM, "phase"));
@@ -787,6 +1006,8 @@ int sph_create(const sph_params* prm, void** out) {
         if ((rc = alloc_state<float>(*c, c->s32))) return cleanup(rc == SPH_ERR_CUDA ? SPH_ERR_NOMEM : rc);
         c->has32 = true;
     }
+    if ((rc = set_fused_attrs())) return cleanup(rc);
+    if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
     if ((rc = init_fields(*c))) return cleanup(rc);
     if ((rc = compute_f_scale(*c))) return cleanup(rc);
@@ -806,6 +1027,11 @@ int sph_destroy(void* h) {
     if (c->hred) cudaFreeHost(c->hred);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
+    for (int i = 0; i < 2; ++i)
+        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
+    if (c->ev2) cudaEventDestroy(c->ev2);
+    if (c->ev3) cudaEventDestroy(c->ev3);
+    if (c->ev4) cudaEventDestroy(c->ev4);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SPH_OK;
@@ -905,6 +1131,7 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
     sph_solve_info* inf = info ? info : &local;
     std::memset(inf, 0, sizeof(*inf));
     auto t0 = std::chrono::steady_clock::now();
+    c->sweep_ms = c->outer_ms = 0.0;
     CK(cudaEventRecord(c->ev0, c->stream));
     int rc;
     const int prec = c->prm.precision;
@@ -933,6 +1160,9 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_ms = ms;
     inf->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    inf->device_ms = ms;
+    inf->sweep_ms = prec == SPH_PREC_MIXED ? c->sweep_ms : ms;
+    inf->outer_ms = c->outer_ms;
     {
         rc = sync64(*c);
         if (rc) return rc;
@@ -942,6 +1172,51 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
         inf->residual = out[6];
     }
     return inf->status;
+}
+
+int sph_sweep(void* h, int64_t k) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (c->prm.precision != SPH_PREC_MIXED) return fail(SPH_ERR_UNSUPPORTED, "sph_sweep needs SPH_PREC_MIXED");
+    if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
+    if (c->prm.rheology == SPH_RHEO_TAU_POWER || c->prm.rheology == SPH_RHEO_TAU_POWER_RELAX)
+        return fail(SPH_ERR_UNSUPPORTED, "mixed precision needs an explicit viscosity law (linear or strain-rate power law)");
+    const int G = c->prm.geometry;
+    int rc;
+    if (!c->corr_ready) {
+        rc = sync64(*c);
+        if (rc) return rc;
+        double out[7];
+        rc = G == SPH ? outer_residual<SPH>(*c, out) : (G == CYL ? outer_residual<CYL>(*c, out) : outer_residual<CART>(*c, out));
+        if (rc) return rc;
+        rc = G == SPH ? prepare_correction<SPH>(*c, out) : (G == CYL ? prepare_correction<CYL>(*c, out) : prepare_correction<CART>(*c, out));
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(c->ev0, c->stream));
+    const int chunk = 100;
+    for (int64_t done = 0; done < k;) {
+        const int m = (int)std::min<int64_t>(chunk, k - done);
+        rc = G == SPH ? run_correction_sweeps<SPH>(*c, m) : (G == CYL ? run_correction_sweeps<CYL>(*c, m) : run_correction_sweeps<CART>(*c, m));
+        if (rc) return rc;
+        done += m;
+    }
+    CK(cudaEventRecord(c->ev1, c->stream));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    c->last_ms = ms;
+    return SPH_OK;
+}
+
+int sph_sweep_apply(void* h) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (!c->corr_ready) return SPH_OK;
+    int rc = apply_correction(*c);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
 }
 
 int sph_residual(void* h, double out[7]) {

@@ -141,3 +141,74 @@ def test_reference_criterion_solve_small():
     assert len(errs) == len(res.hist_err)
     np.testing.assert_allclose(res.hist_err, errs, rtol=1e-6)
     assert errs[-1] < 5e-7 and all(e >= 5e-7 for e in errs[:-1])
+
+
+# ---------------------------------------------------------------------------
+# fused FP32 sweep against the one-kernel-per-step FP32 path and the oracle
+FUSED_CASES = [
+    ("spherical", dict(bc="diapir", n_exp=3.0)),
+    ("spherical", dict(bc="free_slip", rheology="linear")),
+    ("spherical", dict(bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                       sig_bc=(0.0, 0.5, -0.5), incl_linear=1)),
+    ("cylindrical", dict(n_exp=3.0)),
+    ("cartesian", dict(n_exp=3.0)),
+]
+
+
+def _params(geom, n, **kw):
+    if geom == "spherical" and kw.get("bc") in ("free_slip", "stress"):
+        return S.sector_params(n, **kw)
+    return S.default_params(geom, n1=n[0], n2=n[1], n3=n[2], **kw)
+
+
+@pytest.mark.parametrize("geom,kw", FUSED_CASES)
+@pytest.mark.parametrize("n", [(37, 19, 13), (33, 9, 70)])
+def test_fused_equals_simple_fp32(geom, kw, n):
+    k = 30
+    out = {}
+    for variant in ("simple", "auto"):
+        p = _params(geom, n, precision="fp32", kernels=variant, **kw)
+        with S.Solver(p) as sv:
+            sv.step(k)
+            out[variant] = {f: sv.get(f) for f in ("P", "V1", "V2", "V3", "TAU11", "TAU12", "TAU13", "TAU23", "ETA")}
+    for f in out["simple"]:
+        # the same arithmetic in the same order: equal up to FMA-contraction differences
+        assert relerr(out["auto"][f], out["simple"][f]) < 1e-6, f
+
+
+def test_fused_fp32_tracks_fp64_oracle():
+    p = S.default_params("spherical", n1=35, n2=17, n3=21, n_exp=3.0, precision="fp32")
+    k = 40
+    with S.Solver(p) as sv:
+        sv.step(k)
+        got = {f: sv.get(f) for f in ("P", "V1", "V2", "V3", "TAU11", "TAU12")}
+    p.precision = 0
+    o = oracle.Sph.from_params(p)
+    o.iterate(k)
+    for f, g in got.items():
+        assert relerr(g, o.field(f)) < 2e-4, f
+
+
+@pytest.mark.parametrize("passes", [2, 3])
+def test_trajectory_wide_max_filter(passes):
+    p = S.sector_params((15, 13, 11), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5,
+                        edot_bg=0.25, sig_bc=(0.0, 0.5, -0.5), incl_linear=1, etasm_passes=passes)
+    with S.Solver(p) as sv:
+        sv.step(40)
+        o = oracle.Sph.from_params(p)
+        o.iterate(40)
+        compare(o, sv, ("P", "V1", "V2", "V3", "TAU11", "TAU12", "ETA", "ETA_SM"), 1e-9)
+
+
+def test_sweep_graph_equals_plain_sweeps(monkeypatch):
+    """the CUDA-graph replay of correction sweeps gives the sweeps' result"""
+    from bench import workload_params
+    out = []
+    for graphs in ("0", "1"):
+        monkeypatch.setenv("SPH_NO_GRAPHS", "1" if graphs == "0" else "0")
+        with S.Solver(workload_params(31, "mixed")) as sv:
+            sv.sweep(200)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
+    for f in out[0]:
+        assert relerr(out[1][f], out[0][f]) == 0.0, f

@@ -210,6 +210,13 @@ int sph_solve(void* ctx, const sph_solve_opts* opts, sph_solve_info* info,
 int sph_sweep(void* ctx, int64_t k);
 int sph_sweep_apply(void* ctx);
 
+/* MIXED only (no counterpart in the reference: measurement): k sweeps as sph_sweep,
+ * launched one at a time with a CUDA event pair on the library's stream around each
+ * launch of the fused sweep kernel.  *sweep_ms = device time of the k sweeps (fused
+ * kernel + boundary stages), *kernel_ms = summed device time of the k fused-kernel
+ * launches.  Needs SPH_KERNELS_AUTO. */
+int sph_sweep_profile(void* ctx, int64_t k, double* sweep_ms, double* kernel_ms);
+
 /* FP64 Stokes residual of the current state: out[0..2] max|R_mom| per component,
  * out[3] max|div V|, out[4] max|V|, out[5] f_scale, out[6] the SPH_CRIT_RESIDUAL error */
 int sph_residual(void* ctx, double out[7]);

@@ -103,6 +103,7 @@ _SIGS = {
     "sph_residual": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "sph_sweep": ([C.c_void_p, C.c_int64], C.c_int),
     "sph_sweep_apply": ([C.c_void_p], C.c_int),
+    "sph_sweep_profile": ([C.c_void_p, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
     "sph_run_kernel": ([C.c_void_p, C.c_int32], C.c_int),
     "sph_last_device_ms": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "sph_strerror": ([C.c_int], C.c_char_p),
@@ -292,6 +293,13 @@ class Solver:
         """k FP32 sweeps of the current defect-correction step (MIXED); returns their device time in ms."""
         _check(self.lib, self.lib.sph_sweep(self._h, int(k)), "sph_sweep")
         return self.last_device_ms()
+
+    def sweep_profile(self, k: int) -> tuple[float, float]:
+        """k sweeps launched one at a time with events around each fused-kernel launch;
+        returns (device ms of the k sweeps, summed device ms of the fused-kernel launches)."""
+        sw, kn = C.c_double(), C.c_double()
+        _check(self.lib, self.lib.sph_sweep_profile(self._h, int(k), C.byref(sw), C.byref(kn)), "sph_sweep_profile")
+        return float(sw.value), float(kn.value)
 
     def sweep_apply(self) -> None:
         _check(self.lib, self.lib.sph_sweep_apply(self._h), "sph_sweep_apply")

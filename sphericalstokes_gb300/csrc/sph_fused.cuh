@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
 
     // asynchronous loads of one plane (zero fill outside the box / for z outside [0, pz))
     auto issue_inputs = [&](int z) {
-        const int sl = ((z % 3) + 3) % 3;
+        const int sl = (z + 3) % 3;
         const bool zok = z >= 0 && z < d.pz;
         for (int q = tid; q < FLX * FLY; q += FNT) {
             const int lx = q % FLX, ly = q / FLX;
@@ -117,25 +117,39 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
         }
     };
 
+    // per-thread constants of the whole march (see k_fused_tma)
+    const int a = tid % FSX, b = tid / FSX;
+    const int x = x0 - 1 + a, y = y0 - 1 + b;
+    const bool s1_in = tid < FSX * FSY && x >= 0 && y >= 0 && x < n1 && y < n2;
+    const bool s1_own = a >= 1 && b >= 1;
+    const bool e12_xy = x < n1 - 1 && y < n2 - 1, e13_xy = x < n1 - 1 && y < n2 - 2, e23_xy = x < n1 - 2 && y < n2 - 1;
+    const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
+    const EdgeMetric<float> em = edge_metric<float, G>(p.geo, x, y, n1, n2);
+    const int gxy = x + d.sy * y;
+    const int tx = tid % FTX, ty = tid / FTX;
+    const int I = x0 + tx, J = y0 + ty;
+    const bool v_ok = tid < FTX * FTY && I >= 1 && J >= 1 && I <= n1 - 1 && J <= n2 - 1;
+    const bool m1_xy = J <= n2 - 2, m2_xy = I <= n1 - 2, m3_xy = I <= n1 - 2 && J <= n2 - 2;
+    const MomMetric<float> mm = mom_metric<float, G>(p.geo, I, J, n1, n2);
+    const int gIJ = I + d.sy * J;
+
     // stresses of plane k at this thread's stage-1 point; owned points go to the output state
     auto stage1 = [&](int k, bool own_plane) {
         if (tid >= FSX * FSY) return;
-        const int ik = ((k % 3) + 3) % 3, ik1 = (((k + 1) % 3) + 3) % 3, so = k & 1, ol = k & 1;
-        const int a = tid % FSX, b = tid / FSX;
-        const int x = x0 - 1 + a, y = y0 - 1 + b;
-        const bool own = own_plane && a >= 1 && b >= 1;
-        const int g = x + d.sy * y + d.sz * k;
+        const int ik = (k + 3) % 3, ik1 = (k + 4) % 3, so = k & 1, ol = k & 1;
+        const bool own = own_plane && s1_own;
+        const int g = gxy + d.sz * k;
         float (*I0)[FLY][FLX] = S.in[ik];
         float (*I1)[FLY][FLX] = S.in[ik1];
         float (*O)[FSY][FSX] = S.old[ol];
         float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
-        if (x >= 0 && y >= 0 && x < n1 && y < n2) {
+        if (s1_in) {
             {
-                const CellD<float> D = cell_strain<float, G>(p.geo, d1, d2, d3, x, y, I0[0][b][a], I0[0][b][a + 1], I0[1][b][a], I0[1][b + 1][a],
-                                                             I0[2][b][a], I1[2][b][a]);
+                const CellD<float> D = cell_strain_m<float, G>(cm, d1, I0[0][b][a], I0[0][b][a + 1], I0[1][b][a], I0[1][b + 1][a],
+                                                               I0[2][b][a], I1[2][b][a]);
                 const float sm = I0[4][b][a], e = I0[3][b][a];
                 const float gs = gsc * sm, kb = kbc * sm;
-                const float f = e / (e + gs);
+                const float f = pdiv(e, e + gs);
                 float dv = D.div;
                 if (MODE == 1) dv += O[IX][b][a];
                 vP = O[IP][b][a] - kb * dv;
@@ -143,23 +157,23 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
                 v22 = (O[I22][b][a] + 2.f * gs * D.D22) * f;
                 v33 = (O[I33][b][a] + 2.f * gs * D.D33) * f;
                 if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
-                vdt = vpdt2 / (kb + gs * f);
+                vdt = pdiv(vpdt2, kb + gs * f);
                 if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
             }
-            if (x < n1 - 1 && y < n2 - 1 && k < n3 - 2) {
-                const float D = edge12<float, G>(p.geo, d1, d2, x, I1[1][b + 1][a], I1[1][b + 1][a + 1], I1[0][b][a + 1], I1[0][b + 1][a + 1]);
+            if (e12_xy && k < n3 - 2) {
+                const float D = edge12_m<float, G>(em, d1, d2, I1[1][b + 1][a], I1[1][b + 1][a + 1], I1[0][b][a + 1], I1[0][b + 1][a + 1]);
                 v12 = edge_update(O[I12][b][a], gsc, I1[4][b][a] + I1[4][b + 1][a] + I1[4][b][a + 1] + I1[4][b + 1][a + 1],
                                   I1[3][b][a] + I1[3][b + 1][a] + I1[3][b][a + 1] + I1[3][b + 1][a + 1], D);
                 if (own) o.t12[g] = v12;
             }
-            if (x < n1 - 1 && y < n2 - 2 && k < n3 - 1) {
-                const float D = edge13<float, G>(p.geo, d1, d3, x, y, I1[2][b + 1][a], I1[2][b + 1][a + 1], I0[0][b + 1][a + 1], I1[0][b + 1][a + 1]);
+            if (e13_xy && k < n3 - 1) {
+                const float D = edge13_m<float, G>(em, d1, d3, I1[2][b + 1][a], I1[2][b + 1][a + 1], I0[0][b + 1][a + 1], I1[0][b + 1][a + 1]);
                 v13 = edge_update(O[I13][b][a], gsc, I0[4][b + 1][a] + I1[4][b + 1][a] + I0[4][b + 1][a + 1] + I1[4][b + 1][a + 1],
                                   I0[3][b + 1][a] + I1[3][b + 1][a] + I0[3][b + 1][a + 1] + I1[3][b + 1][a + 1], D);
                 if (own) o.t13[g] = v13;
             }
-            if (x < n1 - 2 && y < n2 - 1 && k < n3 - 1) {
-                const float D = edge23<float, G>(p.geo, d2, d3, x, y, I1[2][b][a + 1], I1[2][b + 1][a + 1], I0[1][b + 1][a + 1], I1[1][b + 1][a + 1]);
+            if (e23_xy && k < n3 - 1) {
+                const float D = edge23_m<float, G>(em, d2, d3, I1[2][b][a + 1], I1[2][b + 1][a + 1], I0[1][b + 1][a + 1], I1[1][b + 1][a + 1]);
                 v23 = edge_update(O[I23][b][a], gsc, I0[4][b][a + 1] + I1[4][b][a + 1] + I0[4][b + 1][a + 1] + I1[4][b + 1][a + 1],
                                   I0[3][b][a + 1] + I1[3][b][a + 1] + I0[3][b + 1][a + 1] + I1[3][b + 1][a + 1], D);
                 if (own) o.t23[g] = v23;
@@ -172,11 +186,8 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
 
     // velocities of plane K from the stresses of planes K-1 and K
     auto velocity = [&](int K) {
-        if (tid >= FTX * FTY) return;
-        const int tx = tid % FTX, ty = tid / FTX;
-        const int I = x0 + tx, J = y0 + ty;
-        if (I < 1 || J < 1 || K < 1 || I > n1 - 1 || J > n2 - 1 || K > n3 - 1) return;
-        const int g = I + d.sy * J + d.sz * K;
+        if (!v_ok || K < 1 || K > n3 - 1) return;
+        const int g = gIJ + d.sz * K;
         const float h = 0.5f;
         float (*C0)[FSY][FSX] = S.st[K & 1];
         float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
@@ -184,10 +195,10 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
         const float Pc = C0[IP][ty + 1][tx + 1];
         const float q11 = C0[I11][ty + 1][tx + 1] - Pc, q22 = C0[I22][ty + 1][tx + 1] - Pc, q33 = C0[I33][ty + 1][tx + 1] - Pc;
         const float dtc = C0[IX][ty + 1][tx + 1];
-        if (J <= n2 - 2 && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
+        if (m1_xy && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
             const float Pm = C0[IP][ty + 1][tx];
-            float r = mom1<float, G>(p.geo, d1, d2, d3, I, J, C0[I11][ty + 1][tx] - Pm, q11, C0[I22][ty + 1][tx] - Pm, q22, C0[I33][ty + 1][tx] - Pm,
-                                     q33, C1[I12][ty + 1][tx], C1[I12][ty][tx], C0[I13][ty][tx], C1[I13][ty][tx]);
+            float r = mom1_m<float, G>(mm, d1, d2, d3, C0[I11][ty + 1][tx] - Pm, q11, C0[I22][ty + 1][tx] - Pm, q22, C0[I33][ty + 1][tx] - Pm,
+                                       q33, C1[I12][ty + 1][tx], C1[I12][ty][tx], C0[I13][ty][tx], C1[I13][ty][tx]);
             if (G != CART && MODE == 0) {
                 const float* rho = &S.old[K & 1][IX][0][0];
                 r -= (rho[(ty + 1) * FSX + tx] * p.g + rho[(ty + 1) * FSX + tx + 1] * p.g) * h;
@@ -195,16 +206,16 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
             if (MODE == 1) r += S.rv[K & 1][0][ty][tx];
             o.V1[g] = Vin[0][ty + 1][tx + 1] + r * ((C0[IX][ty + 1][tx] + dtc) * h);
         }
-        if (I <= n1 - 2 && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
+        if (m2_xy && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
             const float Pm = C0[IP][ty][tx + 1];
-            float r = mom2<float, G>(p.geo, d1, d2, d3, I, J, C0[I22][ty][tx + 1] - Pm, q22, C0[I33][ty][tx + 1] - Pm, q33, C1[I12][ty][tx + 1],
-                                     C1[I12][ty][tx], C0[I23][ty][tx], C1[I23][ty][tx]);
+            float r = mom2_m<float, G>(mm, d1, d2, d3, C0[I22][ty][tx + 1] - Pm, q22, C0[I33][ty][tx + 1] - Pm, q33, C1[I12][ty][tx + 1],
+                                       C1[I12][ty][tx], C0[I23][ty][tx], C1[I23][ty][tx]);
             if (MODE == 1) r += S.rv[K & 1][1][ty][tx];
             o.V2[g] = Vin[1][ty + 1][tx + 1] + r * ((C0[IX][ty][tx + 1] + dtc) * h);
         }
-        if (I <= n1 - 2 && J <= n2 - 2) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
-            float r = mom3<float, G>(p.geo, d1, d2, d3, I, J, C1[I33][ty + 1][tx + 1] - C1[IP][ty + 1][tx + 1], q33, C1[I13][ty][tx + 1],
-                                     C1[I13][ty][tx], C1[I23][ty + 1][tx], C1[I23][ty][tx]);
+        if (m3_xy) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
+            float r = mom3_m<float, G>(mm, d1, d2, d3, C1[I33][ty + 1][tx + 1] - C1[IP][ty + 1][tx + 1], q33, C1[I13][ty][tx + 1],
+                                       C1[I13][ty][tx], C1[I23][ty + 1][tx], C1[I23][ty][tx]);
             if (G == CART && MODE == 0) r -= p.g * (h * (p.rho[g - d.sz] + S.old[K & 1][IX][ty + 1][tx + 1]));  // plane K-1's slot is being refilled
             if (MODE == 1) r += S.rv[K & 1][2][ty][tx];
             o.V3[g] = Vin[2][ty + 1][tx + 1] + r * ((C1[IX][ty + 1][tx + 1] + dtc) * h);
@@ -239,5 +250,260 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
 }
 
 inline size_t fused_smem_bytes() { return sizeof(FusedSmem); }
+
+}  // namespace sph
+
+// ===========================================================================
+// TMA variant: the same sweep with the tile loads done by the Tensor Memory
+// Accelerator (cp.async.bulk.tensor.3d, one elected thread per block, mbarrier
+// transaction counts) instead of one cp.async per float.  Tiles start at
+// x0-4 so the innermost coordinate is 16-byte aligned; out-of-range parts of
+// a box (negative or past the end) are zero-filled by the TMA unit.
+#include <cuda.h>
+
+namespace sph {
+
+enum TmaMap {
+    TM_V1 = 0, TM_V2, TM_V3, TM_ETA, TM_ETASM,              // input boxes 40 x 10
+    TM_P, TM_T11, TM_T22, TM_T33, TM_T12, TM_T13, TM_T23,  // old-state boxes 36 x 9
+    TM_RP, TM_RHO,                                          // (36 x 9)
+    TM_RV1, TM_RV2, TM_RV3,                                 // 32 x 8
+    TM_COUNT
+};
+constexpr int TIN_X = 40, TIN_Y = 10, TOLD_X = 36, TOLD_Y = 9;
+constexpr int TIN_TILE = 416;   // floats per input tile (400 used), 1664 B = 13 x 128 B
+constexpr int TOLD_TILE = 352;  // floats per old-state tile (324 used), 1408 B = 11 x 128 B
+constexpr int TRV_TILE = FTX * FTY;
+
+struct TmaSmem {
+    alignas(128) float in[3][F_IN][TIN_TILE];
+    alignas(128) float old[2][F_OLD][TOLD_TILE];
+    alignas(128) float rv[2][F_RV][TRV_TILE];
+    float st[2][8][FSY][FSX];
+    unsigned long long bar_in[3];
+    unsigned long long bar_old[2];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+// bounded wait on the phase with the given parity; false if the bound ran out
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    for (int it = 0; it < (1 << 24); ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load3d(float* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n"
+        ::"r"(smem_u32(dst)), "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <int G, int MODE>
+__global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
+                                                       int* __restrict__ err) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    TmaSmem& S = *reinterpret_cast<TmaSmem*>(smem_raw);
+    enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };
+
+    const Dims d = p.d;
+    const int tid = threadIdx.x;
+    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * FTY;
+    const int kA = blockIdx.z * kchunk;
+    const int kB = min(kA + kchunk, d.n3);
+    const int n1 = d.n1, n2 = d.n2, n3 = d.n3;
+    const float d1 = p.d1, d2 = p.d2, d3 = p.d3, gsc = p.gsc, kbc = p.kbc, vpdt2 = p.vpdt2;
+    if (kA >= kB) return;
+
+    if (tid == 0) {
+        for (int i = 0; i < 3; ++i) mbar_init(&S.bar_in[i], 1);
+        for (int i = 0; i < 2; ++i) mbar_init(&S.bar_old[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+
+    const unsigned in_bytes = F_IN * TIN_X * TIN_Y * 4;
+    const unsigned old_bytes = F_OLD * TOLD_X * TOLD_Y * 4 + (MODE == 1 ? F_RV * FTX * FTY * 4 : 0);
+    auto issue_inputs = [&](int z) {  // thread 0 only
+        const int sl = (z + 3) % 3;
+        mbar_expect_tx(&S.bar_in[sl], in_bytes);
+        for (int f = 0; f < F_IN; ++f) tma_load3d(S.in[sl][f], maps + TM_V1 + f, x0 - 4, y0 - 1, z, &S.bar_in[sl]);
+    };
+    auto issue_old = [&](int z) {  // thread 0 only: old state + rV of plane z
+        const int sl = z & 1;
+        mbar_expect_tx(&S.bar_old[sl], old_bytes);
+        for (int f = 0; f < 7; ++f) tma_load3d(S.old[sl][f], maps + TM_P + f, x0 - 4, y0 - 1, z, &S.bar_old[sl]);
+        tma_load3d(S.old[sl][IX], maps + (MODE == 1 ? TM_RP : TM_RHO), x0 - 4, y0 - 1, z, &S.bar_old[sl]);
+        if (MODE == 1)
+            for (int f = 0; f < F_RV; ++f) tma_load3d(S.rv[sl][f], maps + TM_RV1 + f, x0, y0, z, &S.bar_old[sl]);
+    };
+    unsigned ph_in = 0, ph_old = 0;  // parity bit per ring slot
+    bool ok = true;
+    auto wait_in = [&](int z) {
+        const int sl = (z + 3) % 3;
+        ok &= mbar_wait(&S.bar_in[sl], (ph_in >> sl) & 1u);
+        ph_in ^= 1u << sl;
+    };
+    auto wait_old = [&](int z) {
+        const int sl = z & 1;
+        ok &= mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
+        ph_old ^= 1u << sl;
+    };
+
+    // A thread keeps its stage-1 point (a, b) and its velocity node (tx, ty)
+    // for the whole march: index arithmetic, range tests and metric factors
+    // are computed once, before the first plane.
+    const int a = tid % FSX, b = tid / FSX;
+    const int x = x0 - 1 + a, y = y0 - 1 + b;
+    const bool s1_in = tid < FSX * FSY && x >= 0 && y >= 0 && x < n1 && y < n2;
+    const bool s1_own = a >= 1 && b >= 1;
+    const bool e12_xy = x < n1 - 1 && y < n2 - 1, e13_xy = x < n1 - 1 && y < n2 - 2, e23_xy = x < n1 - 2 && y < n2 - 1;
+    const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
+    const EdgeMetric<float> em = edge_metric<float, G>(p.geo, x, y, n1, n2);
+    const int gxy = x + d.sy * y;
+    const int tx = tid % FTX, ty = tid / FTX;
+    const int I = x0 + tx, J = y0 + ty;
+    const bool v_ok = tid < FTX * FTY && I >= 1 && J >= 1 && I <= n1 - 1 && J <= n2 - 1;
+    const bool m1_xy = J <= n2 - 2, m2_xy = I <= n1 - 2, m3_xy = I <= n1 - 2 && J <= n2 - 2;
+    const MomMetric<float> mm = mom_metric<float, G>(p.geo, I, J, n1, n2);
+    const int gIJ = I + d.sy * J;
+
+    // input tile local (lx, ly) -> in[..][ly*40 + lx + 3]; old tile local (a, b) -> old[..][b*36 + a + 3]
+    auto stage1 = [&](int k, bool own_plane) {
+        if (tid >= FSX * FSY) return;
+        const int ik = (k + 3) % 3, ik1 = (k + 4) % 3, so = k & 1, ol = k & 1;
+        const bool own = own_plane && s1_own;
+        const int g = gxy + d.sz * k;
+        const float* I0[F_IN];
+        const float* I1[F_IN];
+        for (int f = 0; f < F_IN; ++f) { I0[f] = S.in[ik][f] + 3; I1[f] = S.in[ik1][f] + 3; }
+        auto in0 = [&](int f, int bb, int aa) { return I0[f][bb * TIN_X + aa]; };
+        auto in1 = [&](int f, int bb, int aa) { return I1[f][bb * TIN_X + aa]; };
+        const int oi = b * TOLD_X + a + 3;
+        const float* O = &S.old[ol][0][0];
+        auto old = [&](int f) { return O[f * TOLD_TILE + oi]; };
+        float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
+        if (s1_in) {
+            {
+                const CellD<float> D = cell_strain_m<float, G>(cm, d1, in0(0, b, a), in0(0, b, a + 1), in0(1, b, a), in0(1, b + 1, a),
+                                                               in0(2, b, a), in1(2, b, a));
+                const float sm = in0(4, b, a), e = in0(3, b, a);
+                const float gs = gsc * sm, kb = kbc * sm;
+                const float f = pdiv(e, e + gs);
+                float dv = D.div;
+                if (MODE == 1) dv += old(IX);
+                vP = old(IP) - kb * dv;
+                v11 = (old(I11) + 2.f * gs * D.D11) * f;
+                v22 = (old(I22) + 2.f * gs * D.D22) * f;
+                v33 = (old(I33) + 2.f * gs * D.D33) * f;
+                if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
+                vdt = pdiv(vpdt2, kb + gs * f);
+                if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
+            }
+            if (e12_xy && k < n3 - 2) {
+                const float D = edge12_m<float, G>(em, d1, d2, in1(1, b + 1, a), in1(1, b + 1, a + 1), in1(0, b, a + 1), in1(0, b + 1, a + 1));
+                v12 = edge_update(old(I12), gsc, in1(4, b, a) + in1(4, b + 1, a) + in1(4, b, a + 1) + in1(4, b + 1, a + 1),
+                                  in1(3, b, a) + in1(3, b + 1, a) + in1(3, b, a + 1) + in1(3, b + 1, a + 1), D);
+                if (own) o.t12[g] = v12;
+            }
+            if (e13_xy && k < n3 - 1) {
+                const float D = edge13_m<float, G>(em, d1, d3, in1(2, b + 1, a), in1(2, b + 1, a + 1), in0(0, b + 1, a + 1), in1(0, b + 1, a + 1));
+                v13 = edge_update(old(I13), gsc, in0(4, b + 1, a) + in1(4, b + 1, a) + in0(4, b + 1, a + 1) + in1(4, b + 1, a + 1),
+                                  in0(3, b + 1, a) + in1(3, b + 1, a) + in0(3, b + 1, a + 1) + in1(3, b + 1, a + 1), D);
+                if (own) o.t13[g] = v13;
+            }
+            if (e23_xy && k < n3 - 1) {
+                const float D = edge23_m<float, G>(em, d2, d3, in1(2, b, a + 1), in1(2, b + 1, a + 1), in0(1, b + 1, a + 1), in1(1, b + 1, a + 1));
+                v23 = edge_update(old(I23), gsc, in0(4, b, a + 1) + in1(4, b, a + 1) + in0(4, b + 1, a + 1) + in1(4, b + 1, a + 1),
+                                  in0(3, b, a + 1) + in1(3, b, a + 1) + in0(3, b + 1, a + 1) + in1(3, b + 1, a + 1), D);
+                if (own) o.t23[g] = v23;
+            }
+        }
+        float (*W)[FSY][FSX] = S.st[so];
+        W[IP][b][a] = vP; W[I11][b][a] = v11; W[I22][b][a] = v22; W[I33][b][a] = v33;
+        W[I12][b][a] = v12; W[I13][b][a] = v13; W[I23][b][a] = v23; W[IX][b][a] = vdt;
+    };
+
+    auto velocity = [&](int K) {
+        if (!v_ok || K < 1 || K > n3 - 1) return;
+        const int g = gIJ + d.sz * K;
+        const float h = 0.5f;
+        float (*C0)[FSY][FSX] = S.st[K & 1];
+        float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
+        const int vin = (ty + 1) * TIN_X + tx + 4;  // input-tile index of (I, J)
+        const float* Vin = S.in[K % 3][0];
+        const float Pc = C0[IP][ty + 1][tx + 1];
+        const float q11 = C0[I11][ty + 1][tx + 1] - Pc, q22 = C0[I22][ty + 1][tx + 1] - Pc, q33 = C0[I33][ty + 1][tx + 1] - Pc;
+        const float dtc = C0[IX][ty + 1][tx + 1];
+        if (m1_xy && K <= n3 - 2) {
+            const float Pm = C0[IP][ty + 1][tx];
+            float r = mom1_m<float, G>(mm, d1, d2, d3, C0[I11][ty + 1][tx] - Pm, q11, C0[I22][ty + 1][tx] - Pm, q22, C0[I33][ty + 1][tx] - Pm,
+                                       q33, C1[I12][ty + 1][tx], C1[I12][ty][tx], C0[I13][ty][tx], C1[I13][ty][tx]);
+            if (G != CART && MODE == 0) {
+                const float* rho = S.old[K & 1][IX];
+                r -= (rho[(ty + 1) * TOLD_X + tx + 3] * p.g + rho[(ty + 1) * TOLD_X + tx + 4] * p.g) * h;
+            }
+            if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
+            o.V1[g] = Vin[vin] + r * ((C0[IX][ty + 1][tx] + dtc) * h);
+        }
+        if (m2_xy && K <= n3 - 2) {
+            const float Pm = C0[IP][ty][tx + 1];
+            float r = mom2_m<float, G>(mm, d1, d2, d3, C0[I22][ty][tx + 1] - Pm, q22, C0[I33][ty][tx + 1] - Pm, q33, C1[I12][ty][tx + 1],
+                                       C1[I12][ty][tx], C0[I23][ty][tx], C1[I23][ty][tx]);
+            if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
+            o.V2[g] = Vin[TIN_TILE + vin] + r * ((C0[IX][ty][tx + 1] + dtc) * h);
+        }
+        if (m3_xy) {
+            float r = mom3_m<float, G>(mm, d1, d2, d3, C1[I33][ty + 1][tx + 1] - C1[IP][ty + 1][tx + 1], q33, C1[I13][ty][tx + 1],
+                                       C1[I13][ty][tx], C1[I23][ty + 1][tx], C1[I23][ty][tx]);
+            if (G == CART && MODE == 0) r -= p.g * (h * (p.rho[g - d.sz] + S.old[K & 1][IX][(ty + 1) * TOLD_X + tx + 4]));
+            if (MODE == 1) r += S.rv[K & 1][2][ty * FTX + tx];
+            o.V3[g] = Vin[2 * TIN_TILE + vin] + r * ((C1[IX][ty + 1][tx + 1] + dtc) * h);
+        }
+    };
+
+    // prologue: inputs kA-1, kA, kA+1; old kA-1, kA
+    if (tid == 0) {
+        issue_inputs(kA - 1);
+        issue_inputs(kA);
+        issue_old(kA - 1);
+        issue_inputs(kA + 1);
+        issue_old(kA);
+    }
+    wait_in(kA - 1);
+    wait_in(kA);
+    wait_old(kA - 1);
+    if (kA >= 1) stage1(kA - 1, false);
+    for (int K = kA; K < kB; ++K) {
+        __syncthreads();  // every thread is done with the slots of plane K-1
+        if (tid == 0) {
+            issue_inputs(K + 2);
+            issue_old(K + 1);
+        }
+        wait_in(K + 1);
+        wait_old(K);
+        stage1(K, true);
+        __syncthreads();
+        velocity(K);
+    }
+    // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
+    wait_in(kB + 1);
+    wait_old(kB);
+    if (!ok && err) atomicExch(err, 1);
+}
+
+inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }
 
 }  // namespace sph

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(256) k_stress(KP<T> p) {
         const CellD<T> D = cell_strain<T, G>(p.geo, p.d1, p.d2, p.d3, i, j, p.V1[c], p.V1[c + 1], p.V2[c], p.V2[c + sy], p.V3[c], p.V3[c + sz]);
         const T sm = p.etaSM[c], e = p.eta[c];
         const T gs = p.gsc * sm, kb = p.kbc * sm;
-        const T f = e / (e + gs);  // 1/(1 + GSDT/η)
+        const T f = pdiv(e, e + gs);  // 1/(1 + GSDT/η)
         T dv = D.div;
         if (RHS) dv += p.rP[c];
         T Pn = p.P[c] - kb * dv;
@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(256) k_stress(KP<T> p) {
         p.t11[c] = (p.t11[c] + T(2) * gs * D.D11) * f;
         p.t22[c] = n22;
         p.t33[c] = n33;
-        p.DT_R[c] = p.vpdt2 / (kb + gs * f);
+        p.DT_R[c] = pdiv(p.vpdt2, kb + gs * f);
     }
     // τ12 at (i+1/2, j+1/2, k+1): cells (i|i+1, j|j+1, k+1)
     if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {

@@ -4,7 +4,9 @@
 // FP32 state for the FP32 / mixed-precision paths), the metric tables and the
 // boundary-condition program, and drives the PT loop of the reference scripts
 // (SphericalStokes_diapir.jl:409-443) on one CUDA stream.
+#include <cuda.h>
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 
 #include <algorithm>
 #include <chrono>
@@ -87,8 +89,18 @@ struct Ctx {
     float* corr_graph_key[2] = {nullptr, nullptr};   // F_P pointer at capture time
     int graph_len = 0;
     bool use_graphs = true;
+    // TMA tensor maps of the correction sweep, one set per ping-pong arrangement
+    CUtensorMap* d_maps = nullptr;       // [2][TM_COUNT] in device memory
+    float* map_key[2] = {nullptr, nullptr};  // V1 buffer of the arrangement a set was built for
+    int* d_err = nullptr;                // set by a kernel whose bounded wait ran out
+    bool use_tma = true;
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep
+    // per-launch timing of the fused sweep kernel (sph_sweep_profile): event pairs
+    // recorded around each launch while prof_next < prof_ev.size()/2
+    std::vector<cudaEvent_t> prof_ev;
+    size_t prof_next = 0;
+    bool prof_on = false;
 };
 
 constexpr int kRedSlots = 16;
@@ -437,6 +449,11 @@ int fused_chunk(const Ctx& c) {
 }
 
 template <int G, int MODE>
+void set_tma_attr() {
+    cudaFuncSetAttribute(k_fused_tma<G, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
+}
+
+template <int G, int MODE>
 void set_fused_attr() {
     cudaFuncSetAttribute(k_fused<G, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_smem_bytes());
 }
@@ -444,6 +461,7 @@ int set_fused_attrs() {
     set_fused_attr<SPH, 0>(); set_fused_attr<SPH, 1>();
     set_fused_attr<CYL, 0>(); set_fused_attr<CYL, 1>();
     set_fused_attr<CART, 0>(); set_fused_attr<CART, 1>();
+    set_tma_attr<SPH, 1>(); set_tma_attr<CYL, 1>(); set_tma_attr<CART, 1>();
     CK(cudaGetLastError());
     return SPH_OK;
 }
@@ -702,6 +720,85 @@ int prepare_correction(Ctx& c, const double out[7]) {
     return SPH_OK;
 }
 
+// ---------------------------------------------------------------------------
+// TMA tensor maps over the padded box of FP32 fields
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+bool encode_map(const Ctx& c, CUtensorMap* m, const float* base, unsigned bx, unsigned by) {
+    auto enc = tma_encoder();
+    if (!enc) return false;
+    cuuint64_t gdim[3] = {(cuuint64_t)c.d.px, (cuuint64_t)c.d.py, (cuuint64_t)c.d.pz};
+    cuuint64_t gstr[2] = {(cuuint64_t)c.d.px * 4, (cuuint64_t)c.d.px * c.d.py * 4};
+    cuuint32_t box[3] = {bx, by, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), gdim, gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// maps of the current buffer arrangement; returns the device pointer of the set or nullptr
+const CUtensorMap* tma_maps(Ctx& c) {
+    if (!c.use_tma) return nullptr;
+    State<float>& t = c.s32;
+    for (int i = 0; i < 2; ++i)
+        if (c.map_key[i] == t.f[F_V1]) return c.d_maps + i * TM_COUNT;
+    if (!c.d_maps) {
+        if (cudaMalloc((void**)&c.d_maps, sizeof(CUtensorMap) * 2 * TM_COUNT) != cudaSuccess) { c.use_tma = false; return nullptr; }
+        if (cudaMalloc((void**)&c.d_err, sizeof(int)) != cudaSuccess) { c.use_tma = false; return nullptr; }
+        cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream);
+    }
+    const int slot = c.map_key[0] ? 1 : 0;
+    CUtensorMap h[TM_COUNT];
+    const int in_f[5] = {F_V1, F_V2, F_V3, F_ETA, F_ETA_SM};
+    const int old_f[7] = {F_P, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
+    bool ok = true;
+    for (int i = 0; i < 5; ++i) ok &= encode_map(c, &h[TM_V1 + i], t.f[in_f[i]], TIN_X, TIN_Y);
+    for (int i = 0; i < 7; ++i) ok &= encode_map(c, &h[TM_P + i], t.f[old_f[i]], TOLD_X, TOLD_Y);
+    ok &= encode_map(c, &h[TM_RP], t.f[F_RP], TOLD_X, TOLD_Y);
+    ok &= encode_map(c, &h[TM_RHO], t.f[F_RHO], TOLD_X, TOLD_Y);
+    ok &= encode_map(c, &h[TM_RV1], t.f[F_RV1], FTX, FTY);
+    ok &= encode_map(c, &h[TM_RV2], t.f[F_RV2], FTX, FTY);
+    ok &= encode_map(c, &h[TM_RV3], t.f[F_RV3], FTX, FTY);
+    if (!ok || cudaMemcpy(c.d_maps + slot * TM_COUNT, h, sizeof(h), cudaMemcpyHostToDevice) != cudaSuccess) {
+        c.use_tma = false;
+        return nullptr;
+    }
+    c.map_key[slot] = t.f[F_V1];
+    return c.d_maps + slot * TM_COUNT;
+}
+
+// build the tensor-map sets of both ping-pong arrangements (never inside a graph capture)
+void ensure_tma_maps(Ctx& c) {
+    if (!c.use_tma || !c.fused) return;
+    tma_maps(c);
+    swap_state(c.s32);
+    tma_maps(c);
+    swap_state(c.s32);
+}
+
+int check_kernel_flag(Ctx& c) {
+    if (!c.d_err) return SPH_OK;
+    int h = 0;
+    CK(cudaMemcpyAsync(&h, c.d_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    if (h) {
+        CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream));
+        return fail(SPH_ERR_CUDA, "a bounded wait on a TMA barrier ran out in the fused sweep");
+    }
+    return SPH_OK;
+}
+
 // KP of the correction problem: homogeneous boundary data
 KP<float> make_kp_corr(Ctx& c) {
     KP<float> q = make_kp<float>(c, c.s32);
@@ -716,7 +813,23 @@ void correction_sweep(Ctx& c) {
     State<float>& t = c.s32;
     KP<float> q = make_kp_corr(c);
     if (c.fused) {
-        launch_fused<G, 1>(c, q, t);
+        const CUtensorMap* maps = tma_maps(c);
+        if (maps) {
+            FusedOut<float> o;
+            o.P = t.f[F_A_P]; o.V1 = t.f[F_A_V1]; o.V2 = t.f[F_A_V2]; o.V3 = t.f[F_A_V3];
+            o.t11 = t.f[F_A_T11]; o.t22 = t.f[F_A_T22]; o.t33 = t.f[F_A_T33]; o.t12 = t.f[F_A_T12]; o.t13 = t.f[F_A_T13]; o.t23 = t.f[F_A_T23];
+            const int kc = fused_chunk(c);
+            dim3 grid((c.d.n1 + FTX - 1) / FTX, (c.d.n2 + FTY - 1) / FTY, (c.d.n3 + kc - 1) / kc);
+            const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
+            if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next], c.stream);
+            k_fused_tma<G, 1><<<grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
+            if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
+        } else {
+            const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
+            if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next], c.stream);
+            launch_fused<G, 1>(c, q, t);
+            if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
+        }
         swap_state(t);
         q = make_kp_corr(c);
     } else {
@@ -752,6 +865,8 @@ int run_correction_sweeps(Ctx& c, int n) {
     if (slot < 0) {
         slot = c.corr_graph[0] ? 1 : 0;
         if (c.corr_graph[slot]) { cudaGraphExecDestroy(c.corr_graph[slot]); c.corr_graph[slot] = nullptr; }
+        ensure_tma_maps(c);
+        CK(cudaStreamSynchronize(c.stream));
         cudaGraph_t g = nullptr;
         CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
         for (int i = 0; i < n; ++i) correction_sweep<G>(c);  // recorded, not run
@@ -858,6 +973,8 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
             if (ri <= o.inner_rtol * c.corr_r0) break;
         }
         CK(cudaEventRecord(c.ev4, c.stream));
+        rc = check_kernel_flag(c);
+        if (rc) return rc;
         if (status == SPH_ERR_DIVERGED) break;
         rc = apply_correction(c);
         if (rc) return rc;
@@ -1008,6 +1125,7 @@ int sph_create(const sph_params* prm, void** out) {
     }
     if ((rc = set_fused_attrs())) return cleanup(rc);
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
+    if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
     if ((rc = init_fields(*c))) return cleanup(rc);
     if ((rc = compute_f_scale(*c))) return cleanup(rc);
@@ -1023,6 +1141,8 @@ int sph_destroy(void* h) {
     free_state(c->s64);
     free_state(c->s32);
     if (c->phase) cudaFree(c->phase);
+    if (c->d_maps) cudaFree(c->d_maps);
+    if (c->d_err) cudaFree(c->d_err);
     if (c->red) cudaFree(c->red);
     if (c->hred) cudaFreeHost(c->hred);
     if (c->ev0) cudaEventDestroy(c->ev0);
@@ -1032,6 +1152,7 @@ int sph_destroy(void* h) {
     if (c->ev2) cudaEventDestroy(c->ev2);
     if (c->ev3) cudaEventDestroy(c->ev3);
     if (c->ev4) cudaEventDestroy(c->ev4);
+    for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SPH_OK;
@@ -1206,7 +1327,53 @@ int sph_sweep(void* h, int64_t k) {
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_ms = ms;
-    return SPH_OK;
+    return check_kernel_flag(*c);
+}
+
+int sph_sweep_profile(void* h, int64_t k, double* sweep_ms, double* kernel_ms) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !sweep_ms || !kernel_ms) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
+    if (!c->fused) return fail(SPH_ERR_UNSUPPORTED, "sph_sweep_profile times the fused sweep kernel (SPH_KERNELS_AUTO)");
+    *sweep_ms = 0.0;
+    *kernel_ms = 0.0;
+    if (k == 0) return SPH_OK;
+    int rc = sph_sweep(h, 0);  // prepares the correction problem if needed
+    if (rc) return rc;
+    const size_t chunk = 256;  // launches timed between two host synchronisations
+    while (c->prof_ev.size() < 2 * chunk) {
+        cudaEvent_t e;
+        CK(cudaEventCreate(&e));
+        c->prof_ev.push_back(e);
+    }
+    const int G = c->prm.geometry;
+    struct Restore {  // graphs back on and timing off on every return path
+        Ctx* c;
+        bool graphs;
+        ~Restore() { c->use_graphs = graphs; c->prof_on = false; }
+    } restore{c, c->use_graphs};
+    c->use_graphs = false;  // one launch at a time, an event pair around each fused launch
+    c->prof_on = true;
+    for (int64_t done = 0; done < k;) {
+        const int m = (int)std::min<int64_t>((int64_t)chunk, k - done);
+        c->prof_next = 0;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        rc = G == SPH ? run_correction_sweeps<SPH>(*c, m) : (G == CYL ? run_correction_sweeps<CYL>(*c, m) : run_correction_sweeps<CART>(*c, m));
+        if (rc) break;
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        *sweep_ms += ms;
+        for (size_t i = 0; i < c->prof_next; ++i) {
+            CK(cudaEventElapsedTime(&ms, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]));
+            *kernel_ms += ms;
+        }
+        done += m;
+    }
+    if (rc) return rc;
+    c->last_ms = *sweep_ms;
+    return check_kernel_flag(*c);
 }
 
 int sph_sweep_apply(void* h) {

@@ -172,8 +172,9 @@ def test_fused_equals_simple_fp32(geom, kw, n):
             sv.step(k)
             out[variant] = {f: sv.get(f) for f in ("P", "V1", "V2", "V3", "TAU11", "TAU12", "TAU13", "TAU23", "ETA")}
     for f in out["simple"]:
-        # the same arithmetic in the same order: equal up to FMA-contraction differences
-        assert relerr(out["auto"][f], out["simple"][f]) < 1e-6, f
+        # the same expressions, contracted into FMAs differently by the compiler in each
+        # kernel: FP32 rounding differences, amplified by 30 nonlinear iterations
+        assert relerr(out["auto"][f], out["simple"][f]) < 1e-5, f
 
 
 def test_fused_fp32_tracks_fp64_oracle():
@@ -212,3 +213,59 @@ def test_sweep_graph_equals_plain_sweeps(monkeypatch):
             out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
     for f in out[0]:
         assert relerr(out[1][f], out[0][f]) == 0.0, f
+
+
+@pytest.mark.parametrize("n", [31, (40, 17, 23)])
+def test_sweep_tma_equals_cp_async(monkeypatch, n):
+    """the TMA-fed fused correction sweep computes what the cp.async one does (same
+    expressions; FMA contraction may differ between the two kernels)"""
+    from bench import workload_params
+    out = []
+    for tma in ("0", "1"):
+        monkeypatch.setenv("SPH_NO_TMA", "1" if tma == "0" else "0")
+        p = workload_params(31, "mixed") if n == 31 else S.sector_params(n, bc="stress", rheology="edot_power_relax", n_exp=3.0,
+                                                                         relax=0.5, edot_bg=0.25, sig_bc=(0.0, 0.5, -0.5),
+                                                                         incl_linear=1, precision="mixed")
+        with S.Solver(p) as sv:
+            sv.sweep(57)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
+    for f in out[0]:
+        assert relerr(out[1][f], out[0][f]) < 1e-5, f
+
+
+def test_sweep_profile_equals_sweeps():
+    """per-launch timed sweeps compute what the graph-replayed sweeps compute"""
+    from bench import workload_params
+    out, times = [], None
+    for prof in (False, True):
+        with S.Solver(workload_params(31, "mixed")) as sv:
+            if prof:
+                times = sv.sweep_profile(200)
+            else:
+                sv.sweep(200)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
+    for f in out[0]:
+        assert relerr(out[1][f], out[0][f]) == 0.0, f
+    sweep_ms, kernel_ms = times
+    assert 0.0 < kernel_ms <= sweep_ms
+
+
+def test_mixed_solution_matches_fp64():
+    """FP32 sweeps inside FP64 defect correction reach the FP64 PT solution: both to
+    FP64 residual 1e-8, relative velocity difference <= 1e-6"""
+    from bench import workload_params
+    vel = {}
+    for prec in ("fp64", "mixed"):
+        with S.Solver(workload_params(23, prec, tuned=True)) as sv:
+            if prec == "mixed":
+                r = sv.solve(tol=1e-8, maxiter=400_000, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=60,
+                             inner_max=100_000, warm_tol=1e-5)
+            else:
+                r = sv.solve(tol=1e-8, maxiter=400_000, nout=500, criterion="residual")
+            assert r.converged and r.residual < 1e-8, (prec, r.status, r.residual)
+            vel[prec] = [sv.get(f) for f in ("V1", "V2", "V3")]
+    vmax = max(np.abs(v).max() for v in vel["fp64"])
+    err = max(np.abs(a - b).max() for a, b in zip(vel["mixed"], vel["fp64"])) / vmax
+    assert err <= 1e-6, err

@@ -279,7 +279,7 @@ struct TmaSmem {
     alignas(128) float in[3][F_IN][TIN_TILE];
     alignas(128) float old[2][F_OLD][TOLD_TILE];
     alignas(128) float rv[2][F_RV][TRV_TILE];
-    float st[2][8][FSY][FSX];
+    float st[2][7][FSY][FSX];  // τ11-P, τ22-P, τ33-P, τ12, τ13, τ23, DT_R of planes K-1, K
     unsigned long long bar_in[3];
     unsigned long long bar_old[2];
 };
@@ -311,12 +311,19 @@ __device__ __forceinline__ void tma_load3d(float* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// Thread roles (10 warps): warp w < 8 owns the row J = y0 + w of the tile, lane
+// l the column I = x0 + l: it computes the stage-1 point (I, J) (a = l+1,
+// b = w+1) and then the velocity node (I, J), taking its own point's stresses,
+// step and velocities from registers.  Warp 8 computes the low-x2 halo row
+// (b = 0), lanes 0..8 of warp 9 the low-x1 halo column (a = 0).  Shared-memory
+// rows are then read by whole warps at consecutive addresses.
 template <int G, int MODE>
 __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
                                                        int* __restrict__ err) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TmaSmem& S = *reinterpret_cast<TmaSmem*>(smem_raw);
-    enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };
+    enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-tile slots (IX: rP | ρ)
+    enum { Q11 = 0, Q22, Q33, E12, E13, E23, QDT };     // stress-ring slots
 
     const Dims d = p.d;
     const int tid = threadIdx.x;
@@ -362,44 +369,47 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         ph_old ^= 1u << sl;
     };
 
-    // A thread keeps its stage-1 point (a, b) and its velocity node (tx, ty)
-    // for the whole march: index arithmetic, range tests and metric factors
-    // are computed once, before the first plane.
-    const int a = tid % FSX, b = tid / FSX;
+    // per-thread constants of the whole march
+    const int warp = tid >> 5, lane = tid & 31;
+    const int a = warp < FTY ? lane + 1 : (warp == FTY ? lane + 1 : 0);
+    const int b = warp < FTY ? warp + 1 : (warp == FTY ? 0 : lane);
+    const bool s1_thread = warp <= FTY || lane <= FTY;
     const int x = x0 - 1 + a, y = y0 - 1 + b;
-    const bool s1_in = tid < FSX * FSY && x >= 0 && y >= 0 && x < n1 && y < n2;
-    const bool s1_own = a >= 1 && b >= 1;
+    const bool s1_in = s1_thread && x >= 0 && y >= 0 && x < n1 && y < n2;
+    const bool s1_own = warp < FTY;
     const bool e12_xy = x < n1 - 1 && y < n2 - 1, e13_xy = x < n1 - 1 && y < n2 - 2, e23_xy = x < n1 - 2 && y < n2 - 1;
     const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
     const EdgeMetric<float> em = edge_metric<float, G>(p.geo, x, y, n1, n2);
     const int gxy = x + d.sy * y;
-    const int tx = tid % FTX, ty = tid / FTX;
+    const int iin = b * TIN_X + a + 3;   // input-tile index of the stage-1 point
+    const int iold = b * TOLD_X + a + 3; // old-tile index of the stage-1 point
+    const int tx = lane, ty = warp;      // velocity node (warps < FTY)
     const int I = x0 + tx, J = y0 + ty;
-    const bool v_ok = tid < FTX * FTY && I >= 1 && J >= 1 && I <= n1 - 1 && J <= n2 - 1;
+    const bool v_ok = warp < FTY && I >= 1 && J >= 1 && I <= n1 - 1 && J <= n2 - 1;
     const bool m1_xy = J <= n2 - 2, m2_xy = I <= n1 - 2, m3_xy = I <= n1 - 2 && J <= n2 - 2;
     const MomMetric<float> mm = mom_metric<float, G>(p.geo, I, J, n1, n2);
     const int gIJ = I + d.sy * J;
 
-    // input tile local (lx, ly) -> in[..][ly*40 + lx + 3]; old tile local (a, b) -> old[..][b*36 + a + 3]
+    // this thread's stage-1 point of the current plane, and carried values of the previous plane
+    float o11 = 0.f, o22 = 0.f, o33 = 0.f, odt = 0.f, ov1 = 0.f, ov2 = 0.f, ov3 = 0.f;
+    float p33 = 0.f, pdt = 0.f, p13 = 0.f, p23 = 0.f;
+
     auto stage1 = [&](int k, bool own_plane) {
-        if (tid >= FSX * FSY) return;
-        const int ik = (k + 3) % 3, ik1 = (k + 4) % 3, so = k & 1, ol = k & 1;
+        if (!s1_thread) return;
+        const float* I0 = S.in[(k + 3) % 3][0] + iin;
+        const float* I1 = S.in[(k + 4) % 3][0] + iin;
+        auto in0 = [&](int f, int db, int da) { return I0[f * TIN_TILE + db * TIN_X + da]; };
+        auto in1 = [&](int f, int db, int da) { return I1[f * TIN_TILE + db * TIN_X + da]; };
+        const float* O = &S.old[k & 1][0][0] + iold;
+        auto old = [&](int f) { return O[f * TOLD_TILE]; };
         const bool own = own_plane && s1_own;
         const int g = gxy + d.sz * k;
-        const float* I0[F_IN];
-        const float* I1[F_IN];
-        for (int f = 0; f < F_IN; ++f) { I0[f] = S.in[ik][f] + 3; I1[f] = S.in[ik1][f] + 3; }
-        auto in0 = [&](int f, int bb, int aa) { return I0[f][bb * TIN_X + aa]; };
-        auto in1 = [&](int f, int bb, int aa) { return I1[f][bb * TIN_X + aa]; };
-        const int oi = b * TOLD_X + a + 3;
-        const float* O = &S.old[ol][0][0];
-        auto old = [&](int f) { return O[f * TOLD_TILE + oi]; };
         float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
         if (s1_in) {
             {
-                const CellD<float> D = cell_strain_m<float, G>(cm, d1, in0(0, b, a), in0(0, b, a + 1), in0(1, b, a), in0(1, b + 1, a),
-                                                               in0(2, b, a), in1(2, b, a));
-                const float sm = in0(4, b, a), e = in0(3, b, a);
+                ov1 = in0(0, 0, 0); ov2 = in0(1, 0, 0); ov3 = in0(2, 0, 0);
+                const CellD<float> D = cell_strain_m<float, G>(cm, d1, ov1, in0(0, 0, 1), ov2, in0(1, 1, 0), ov3, in1(2, 0, 0));
+                const float sm = in0(4, 0, 0), e = in0(3, 0, 0);
                 const float gs = gsc * sm, kb = kbc * sm;
                 const float f = pdiv(e, e + gs);
                 float dv = D.div;
@@ -413,65 +423,60 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
                 if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
             }
             if (e12_xy && k < n3 - 2) {
-                const float D = edge12_m<float, G>(em, d1, d2, in1(1, b + 1, a), in1(1, b + 1, a + 1), in1(0, b, a + 1), in1(0, b + 1, a + 1));
-                v12 = edge_update(old(I12), gsc, in1(4, b, a) + in1(4, b + 1, a) + in1(4, b, a + 1) + in1(4, b + 1, a + 1),
-                                  in1(3, b, a) + in1(3, b + 1, a) + in1(3, b, a + 1) + in1(3, b + 1, a + 1), D);
+                const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
+                v12 = edge_update(old(I12), gsc, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
+                                  in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
                 if (own) o.t12[g] = v12;
             }
             if (e13_xy && k < n3 - 1) {
-                const float D = edge13_m<float, G>(em, d1, d3, in1(2, b + 1, a), in1(2, b + 1, a + 1), in0(0, b + 1, a + 1), in1(0, b + 1, a + 1));
-                v13 = edge_update(old(I13), gsc, in0(4, b + 1, a) + in1(4, b + 1, a) + in0(4, b + 1, a + 1) + in1(4, b + 1, a + 1),
-                                  in0(3, b + 1, a) + in1(3, b + 1, a) + in0(3, b + 1, a + 1) + in1(3, b + 1, a + 1), D);
+                const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
+                v13 = edge_update(old(I13), gsc, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
+                                  in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
                 if (own) o.t13[g] = v13;
             }
             if (e23_xy && k < n3 - 1) {
-                const float D = edge23_m<float, G>(em, d2, d3, in1(2, b, a + 1), in1(2, b + 1, a + 1), in0(1, b + 1, a + 1), in1(1, b + 1, a + 1));
-                v23 = edge_update(old(I23), gsc, in0(4, b, a + 1) + in1(4, b, a + 1) + in0(4, b + 1, a + 1) + in1(4, b + 1, a + 1),
-                                  in0(3, b, a + 1) + in1(3, b, a + 1) + in0(3, b + 1, a + 1) + in1(3, b + 1, a + 1), D);
+                const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
+                v23 = edge_update(old(I23), gsc, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
+                                  in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
                 if (own) o.t23[g] = v23;
             }
         }
-        float (*W)[FSY][FSX] = S.st[so];
-        W[IP][b][a] = vP; W[I11][b][a] = v11; W[I22][b][a] = v22; W[I33][b][a] = v33;
-        W[I12][b][a] = v12; W[I13][b][a] = v13; W[I23][b][a] = v23; W[IX][b][a] = vdt;
+        o11 = v11 - vP; o22 = v22 - vP; o33 = v33 - vP; odt = vdt;
+        float (*W)[FSY][FSX] = S.st[k & 1];
+        W[Q11][b][a] = o11; W[Q22][b][a] = o22; W[Q33][b][a] = o33;
+        W[E12][b][a] = v12; W[E13][b][a] = v13; W[E23][b][a] = v23; W[QDT][b][a] = vdt;
     };
 
+    // velocities of plane K from the stresses of planes K-1 and K
     auto velocity = [&](int K) {
-        if (!v_ok || K < 1 || K > n3 - 1) return;
-        const int g = gIJ + d.sz * K;
-        const float h = 0.5f;
+        if (!v_ok) return;
         float (*C0)[FSY][FSX] = S.st[K & 1];
         float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
-        const int vin = (ty + 1) * TIN_X + tx + 4;  // input-tile index of (I, J)
-        const float* Vin = S.in[K % 3][0];
-        const float Pc = C0[IP][ty + 1][tx + 1];
-        const float q11 = C0[I11][ty + 1][tx + 1] - Pc, q22 = C0[I22][ty + 1][tx + 1] - Pc, q33 = C0[I33][ty + 1][tx + 1] - Pc;
-        const float dtc = C0[IX][ty + 1][tx + 1];
-        if (m1_xy && K <= n3 - 2) {
-            const float Pm = C0[IP][ty + 1][tx];
-            float r = mom1_m<float, G>(mm, d1, d2, d3, C0[I11][ty + 1][tx] - Pm, q11, C0[I22][ty + 1][tx] - Pm, q22, C0[I33][ty + 1][tx] - Pm,
-                                       q33, C1[I12][ty + 1][tx], C1[I12][ty][tx], C0[I13][ty][tx], C1[I13][ty][tx]);
-            if (G != CART && MODE == 0) {
-                const float* rho = S.old[K & 1][IX];
-                r -= (rho[(ty + 1) * TOLD_X + tx + 3] * p.g + rho[(ty + 1) * TOLD_X + tx + 4] * p.g) * h;
+        if (K == kA) { p13 = C1[E13][ty][tx]; p23 = C1[E23][ty][tx]; }
+        const float c13 = C0[E13][ty][tx], c23 = C0[E23][ty][tx];
+        if (K >= 1 && K <= n3 - 1) {
+            const int g = gIJ + d.sz * K;
+            const float h = 0.5f;
+            const float t12a = C1[E12][ty + 1][tx], t12b = C1[E12][ty][tx];
+            if (m1_xy && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
+                float r = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
+                                           t12a, t12b, c13, p13);
+                if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
+                o.V1[g] = ov1 + r * ((C0[QDT][ty + 1][tx] + odt) * h);
             }
-            if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
-            o.V1[g] = Vin[vin] + r * ((C0[IX][ty + 1][tx] + dtc) * h);
+            if (m2_xy && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
+                float r = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
+                                           c23, p23);
+                if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
+                o.V2[g] = ov2 + r * ((C0[QDT][ty][tx + 1] + odt) * h);
+            }
+            if (m3_xy) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
+                float r = mom3_m<float, G>(mm, d1, d2, d3, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
+                if (MODE == 1) r += S.rv[K & 1][2][ty * FTX + tx];
+                o.V3[g] = ov3 + r * ((pdt + odt) * h);
+            }
         }
-        if (m2_xy && K <= n3 - 2) {
-            const float Pm = C0[IP][ty][tx + 1];
-            float r = mom2_m<float, G>(mm, d1, d2, d3, C0[I22][ty][tx + 1] - Pm, q22, C0[I33][ty][tx + 1] - Pm, q33, C1[I12][ty][tx + 1],
-                                       C1[I12][ty][tx], C0[I23][ty][tx], C1[I23][ty][tx]);
-            if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
-            o.V2[g] = Vin[TIN_TILE + vin] + r * ((C0[IX][ty][tx + 1] + dtc) * h);
-        }
-        if (m3_xy) {
-            float r = mom3_m<float, G>(mm, d1, d2, d3, C1[I33][ty + 1][tx + 1] - C1[IP][ty + 1][tx + 1], q33, C1[I13][ty][tx + 1],
-                                       C1[I13][ty][tx], C1[I23][ty + 1][tx], C1[I23][ty][tx]);
-            if (G == CART && MODE == 0) r -= p.g * (h * (p.rho[g - d.sz] + S.old[K & 1][IX][(ty + 1) * TOLD_X + tx + 4]));
-            if (MODE == 1) r += S.rv[K & 1][2][ty * FTX + tx];
-            o.V3[g] = Vin[2 * TIN_TILE + vin] + r * ((C1[IX][ty + 1][tx + 1] + dtc) * h);
-        }
+        p13 = c13; p23 = c23; p33 = o33; pdt = odt;
     };
 
     // prologue: inputs kA-1, kA, kA+1; old kA-1, kA
@@ -485,7 +490,11 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     wait_in(kA - 1);
     wait_in(kA);
     wait_old(kA - 1);
-    if (kA >= 1) stage1(kA - 1, false);
+    if (kA >= 1) {
+        stage1(kA - 1, false);
+        p33 = o33;
+        pdt = odt;
+    }
     for (int K = kA; K < kB; ++K) {
         __syncthreads();  // every thread is done with the slots of plane K-1
         if (tid == 0) {

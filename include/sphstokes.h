@@ -217,6 +217,21 @@ int sph_sweep_apply(void* ctx);
  * launches.  Needs SPH_KERNELS_AUTO. */
 int sph_sweep_profile(void* ctx, int64_t k, double* sweep_ms, double* kernel_ms);
 
+/* Allocation-free exit check (no counterpart in the reference's interface: it restates
+ * the reference's own check, check_err! and the three maximum(abs.(.)) ratios of
+ * SphericalStokes_diapir.jl:332-344, :428-432, for caller-owned device arrays).
+ * v[i], v_old[i]: DEVICE pointers to count[i] doubles each (any layout); i < m, with
+ * 1 <= m <= SPH_NOALLOC_MAX_ARRAYS, beyond which it returns SPH_ERR_INVALID and
+ * launches nothing.  *err (host) = max_i max|v[i] - v_old[i]| / max|v[i]|.  Work is
+ * queued on `stream` (NULL: the legacy default stream), which the call synchronizes.
+ * It allocates no memory: its reduction slots are a static device array of
+ * 2 * SPH_NOALLOC_MAX_ARRAYS * 8 bytes shared by every call, so calls that overlap on
+ * the GPU race.  The first call on a device looks the array up (cudaGetSymbolAddress)
+ * with that device current; make that first call before any stream capture. */
+#define SPH_NOALLOC_MAX_ARRAYS 8
+int sph_check_err_noalloc(int32_t m, const double* const* v, const double* const* v_old, const int64_t* count, double* err,
+                          void* stream);
+
 /* FP64 Stokes residual of the current state: out[0..2] max|R_mom| per component,
  * out[3] max|div V|, out[4] max|V|, out[5] f_scale, out[6] the SPH_CRIT_RESIDUAL error */
 int sph_residual(void* ctx, double out[7]);

@@ -108,6 +108,8 @@ _SIGS = {
     "sph_last_device_ms": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "sph_strerror": ([C.c_int], C.c_char_p),
     "sph_last_error": ([], C.c_char_p),
+    "sph_check_err_noalloc": ([C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
+                               C.POINTER(C.c_double), C.c_void_p], C.c_int),
 }
 
 _lib = None

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -1434,6 +1435,82 @@ int sph_last_device_ms(void* h, double* ms) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !ms) return fail(SPH_ERR_INVALID, "NULL argument");
     *ms = c->last_ms;
+    return SPH_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free exit check.  The scratch of k_maxabs (one reduction slot per
+// array and quantity: [0, m) max|v - v_old|, [m, 2m) max|v|) is this static
+// array instead of the context's cudaMalloc'd slots; every device that loads
+// the library holds it (2 * SPH_NOALLOC_MAX_ARRAYS * 8 bytes) until exit.  All
+// calls share it: each call clears the slots it uses before its reductions, so
+// calls whose work overlaps on the GPU (other streams, other host threads) race.
+static __device__ __align__(256) unsigned long long g_noalloc_red[2 * SPH_NOALLOC_MAX_ARRAYS];
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};  // device address of g_noalloc_red, per device
+
+// once per device, with that device current: the device address of the static scratch
+int noalloc_scratch(unsigned long long** out) {
+    int dev = -1;
+    CK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(SPH_ERR_UNSUPPORTED, "sph_check_err_noalloc: device ordinal beyond 63");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* a = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_red);
+        if (e != cudaSuccess || !a)
+            return fail(SPH_ERR_CUDA, std::string("sph_check_err_noalloc: cudaGetSymbolAddress of the static scratch: ") +
+                                          cudaGetErrorString(e));
+        g_noalloc_addr[dev] = static_cast<unsigned long long*>(a);
+    }
+    *out = g_noalloc_addr[dev];
+    return SPH_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sph_check_err_noalloc(int32_t m, const double* const* v, const double* const* v_old, const int64_t* count, double* err,
+                          void* stream) {
+    if (!v || !v_old || !count || !err) return fail(SPH_ERR_INVALID, "sph_check_err_noalloc: NULL argument");
+    if (m < 1 || m > SPH_NOALLOC_MAX_ARRAYS)
+        return fail(SPH_ERR_INVALID, "sph_check_err_noalloc: m = " + std::to_string(m) + " arrays; its static scratch holds 1 to " +
+                                         std::to_string(SPH_NOALLOC_MAX_ARRAYS));
+    for (int i = 0; i < m; ++i) {
+        if (!v[i] || !v_old[i]) return fail(SPH_ERR_INVALID, "sph_check_err_noalloc: NULL array pointer");
+        if (count[i] < 1) return fail(SPH_ERR_INVALID, "sph_check_err_noalloc: count < 1");
+    }
+    unsigned long long* slots = nullptr;
+    int rc = noalloc_scratch(&slots);
+    if (rc) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    CK(cudaMemsetAsync(slots, 0, sizeof(unsigned long long) * 2 * m, st));  // max-reductions start at 0
+    for (int i = 0; i < m; ++i) {
+        k_maxabs<double><<<ew_blocks(count[i]), 256, 0, st>>>(v[i], v_old[i], count[i], slots + i);
+        k_maxabs<double><<<ew_blocks(count[i]), 256, 0, st>>>(v[i], nullptr, count[i], slots + m + i);
+    }
+    CK(cudaGetLastError());
+    unsigned long long h[2 * SPH_NOALLOC_MAX_ARRAYS];
+    CK(cudaMemcpyAsync(h, slots, sizeof(unsigned long long) * 2 * m, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    // err = max_i max|v_i - v_old_i| / max|v_i| with NaN propagation (Julia's max)
+    double e = 0.0;
+    for (int i = 0; i < m; ++i) {
+        double dv, vv;
+        std::memcpy(&dv, &h[i], sizeof(double));
+        std::memcpy(&vv, &h[m + i], sizeof(double));
+        const double r = dv / vv;
+        if (!(r == r)) { e = r; break; }
+        e = std::max(e, r);
+    }
+    *err = e;
     return SPH_OK;
 }
 

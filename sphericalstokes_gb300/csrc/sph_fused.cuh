@@ -292,14 +292,19 @@ __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned coun
 __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
-// bounded wait on the phase with the given parity; false if the bound ran out
+// bounded wait on the phase with the given parity; false if the bound ran out.
+// Each try_wait suspends the thread until the phase completes or kMbarSuspendNs
+// pass, so a waiting warp does not re-issue polls; kMbarMaxPolls of them bound
+// the wait to about 2 s.
+constexpr unsigned kMbarSuspendNs = 200000;
+constexpr int kMbarMaxPolls = 10000;
 __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
     const unsigned a = smem_u32(bar);
-    for (int it = 0; it < (1 << 24); ++it) {
+    for (int it = 0; it < kMbarMaxPolls; ++it) {
         unsigned done;
         asm volatile(
-            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done) : "r"(a), "r"(parity) : "memory");
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done) : "r"(a), "r"(parity), "r"(kMbarSuspendNs) : "memory");
         if (done) return true;
     }
     return false;

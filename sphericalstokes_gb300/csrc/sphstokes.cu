@@ -21,6 +21,7 @@
 
 #include "sph_pt.cuh"
 #include "sph_fused.cuh"
+#include "sph_sweep_x2.cuh"
 #include "sphstokes.h"
 
 using namespace sph;
@@ -95,6 +96,7 @@ struct Ctx {
     float* map_key[2] = {nullptr, nullptr};  // V1 buffer of the arrangement a set was built for
     int* d_err = nullptr;                // set by a kernel whose bounded wait ran out
     bool use_tma = true;
+    bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep
     // per-launch timing of the fused sweep kernel (sph_sweep_profile): event pairs
@@ -463,6 +465,9 @@ int set_fused_attrs() {
     set_fused_attr<CYL, 0>(); set_fused_attr<CYL, 1>();
     set_fused_attr<CART, 0>(); set_fused_attr<CART, 1>();
     set_tma_attr<SPH, 1>(); set_tma_attr<CYL, 1>(); set_tma_attr<CART, 1>();
+    cudaFuncSetAttribute(k_sweep_x2<SPH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
+    cudaFuncSetAttribute(k_sweep_x2<CYL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
+    cudaFuncSetAttribute(k_sweep_x2<CART>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
     CK(cudaGetLastError());
     return SPH_OK;
 }
@@ -823,7 +828,10 @@ void correction_sweep(Ctx& c) {
             dim3 grid((c.d.n1 + FTX - 1) / FTX, (c.d.n2 + FTY - 1) / FTY, (c.d.n3 + kc - 1) / kc);
             const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next], c.stream);
-            k_fused_tma<G, 1><<<grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
+            if (c.use_x2)
+                k_sweep_x2<G><<<grid, dim3(X2_NT, 1, 1), sweep_x2_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
+            else
+                k_fused_tma<G, 1><<<grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
         } else {
             const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
@@ -1127,6 +1135,7 @@ int sph_create(const sph_params* prm, void** out) {
     if ((rc = set_fused_attrs())) return cleanup(rc);
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
+    if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
     if ((rc = init_fields(*c))) return cleanup(rc);
     if ((rc = compute_f_scale(*c))) return cleanup(rc);

@@ -269,3 +269,31 @@ def test_mixed_solution_matches_fp64():
     vmax = max(np.abs(v).max() for v in vel["fp64"])
     err = max(np.abs(a - b).max() for a, b in zip(vel["mixed"], vel["fp64"])) / vmax
     assert err <= 1e-6, err
+
+
+X2_CASES = [
+    ("spherical", 31, dict(bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                           sig_bc=(0.0, 0.5, -0.5), incl_linear=1)),
+    ("spherical", (40, 17, 23), dict(bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                                     sig_bc=(0.0, 0.5, -0.5), incl_linear=1)),
+    ("spherical", (33, 9, 21), dict(bc="free_slip", rheology="linear")),
+    ("cylindrical", (35, 11, 19), dict(rheology="linear")),
+    ("cartesian", (31, 13, 17), dict(rheology="linear")),
+]
+
+
+@pytest.mark.parametrize("geom,n,kw", X2_CASES)
+def test_sweep_two_points_per_thread_equals_one(monkeypatch, geom, n, kw):
+    """the paired-arithmetic TMA sweep (two x1-adjacent points per thread) computes what the
+    one-point-per-thread TMA sweep does, up to FP32 rounding of the fused multiply-adds"""
+    out = []
+    for x2 in ("0", "1"):
+        monkeypatch.setenv("SPH_SWEEP_X2", x2)
+        nn = (n, n, n) if isinstance(n, int) else n
+        p = _params(geom, nn, precision="mixed", **kw)
+        with S.Solver(p) as sv:
+            sv.sweep(57)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
+    for f in out[0]:
+        assert relerr(out[1][f], out[0][f]) < 1e-5, f

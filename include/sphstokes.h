@@ -217,6 +217,17 @@ int sph_sweep_apply(void* ctx);
  * launches.  Needs SPH_KERNELS_AUTO. */
 int sph_sweep_profile(void* ctx, int64_t k, double* sweep_ms, double* kernel_ms);
 
+/* Writes the results in the scripts' output format (Save_infos, Save_phys, SaveArray,
+ * SphericalStokes_diapir.jl:23-43, :461-485; CylindricalStokes_diapir.jl:18-37, :390-419;
+ * CartesianStokes_diapir.jl:18-37, :404-425) into the directory `dir` (created if absent):
+ * <num>_infos.inf, <num>_phys.inf and A_<name>.bin (raw little-endian Float64, column-major,
+ * the scripts' array sizes): the coordinate grids, ETAS, RHO, P, the velocities, the six
+ * stresses, TII, err_evo and iter_evo (from hist_*, nhist entries; NULL when nhist = 0),
+ * and for cylindrical geometry RHOG, DIVV and D_* of the current velocities.  tol and
+ * runtime_s fill the εnonl and run-time entries of <num>_infos.inf. */
+int sph_save(void* ctx, const char* dir, int32_t num, double tol, double runtime_s, const int64_t* hist_iter,
+             const double* hist_err, int64_t nhist);
+
 /* Allocation-free exit check (no counterpart in the reference's interface: it restates
  * the reference's own check, check_err! and the three maximum(abs.(.)) ratios of
  * SphericalStokes_diapir.jl:332-344, :428-432, for caller-owned device arrays).

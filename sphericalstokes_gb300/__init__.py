@@ -108,6 +108,8 @@ _SIGS = {
     "sph_last_device_ms": ([C.c_void_p, C.POINTER(C.c_double)], C.c_int),
     "sph_strerror": ([C.c_int], C.c_char_p),
     "sph_last_error": ([], C.c_char_p),
+    "sph_save": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                  C.c_int64], C.c_int),
     "sph_check_err_noalloc": ([C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
                                C.POINTER(C.c_double), C.c_void_p], C.c_int),
 }
@@ -295,6 +297,16 @@ class Solver:
         """k FP32 sweeps of the current defect-correction step (MIXED); returns their device time in ms."""
         _check(self.lib, self.lib.sph_sweep(self._h, int(k)), "sph_sweep")
         return self.last_device_ms()
+
+    def save(self, folder: str | os.PathLike, num: int = 1, tol: float = 5e-7, runtime: float = 0.0,
+             result: SolveResult | None = None) -> None:
+        """Write the fields in the scripts' output format (``<num>_infos.inf``, ``<num>_phys.inf``,
+        ``A_<name>.bin``) into ``folder``; ``result`` supplies err_evo / iter_evo."""
+        hi = np.ascontiguousarray(result.hist_iter if result is not None else np.zeros(0), dtype=np.int64)
+        he = np.ascontiguousarray(result.hist_err if result is not None else np.zeros(0), dtype=np.float64)
+        _check(self.lib, self.lib.sph_save(self._h, os.fsencode(str(folder)), int(num), float(tol), float(runtime),
+                                           hi.ctypes.data_as(C.POINTER(C.c_int64)), he.ctypes.data_as(C.POINTER(C.c_double)),
+                                           len(hi)), "sph_save")
 
     def sweep_profile(self, k: int) -> tuple[float, float]:
         """k sweeps launched one at a time with events around each fused-kernel launch;

@@ -86,6 +86,35 @@ __global__ void __launch_bounds__(256) k_stress(KP<T> p) {
 }
 
 // ---------------------------------------------------------------------------
+// strain rates of the current velocities as separate fields (the DIVV and D_*
+// arrays compute_P! fills in CylindricalStokes_diapir.jl:153-159): divergence
+// and normal rates at cells, engineering shear rates at the three edge sets,
+// in the layout of P and τ12, τ13, τ23.
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_strain_out(KP<T> p, T* __restrict__ dv, T* __restrict__ d11, T* __restrict__ d22,
+                                                    T* __restrict__ d33, T* __restrict__ d12, T* __restrict__ d13, T* __restrict__ d23) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const CellD<T> D = cell_strain<T, G>(p.geo, p.d1, p.d2, p.d3, i, j, p.V1[c], p.V1[c + 1], p.V2[c], p.V2[c + sy], p.V3[c], p.V3[c + sz]);
+    dv[c] = D.div; d11[c] = D.D11; d22[c] = D.D22; d33[c] = D.D33;
+    if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) {
+        const int q = c + sz;
+        d12[c] = edge12<T, G>(p.geo, p.d1, p.d2, i, p.V2[q + sy], p.V2[q + sy + 1], p.V1[q + 1], p.V1[q + 1 + sy]);
+    }
+    if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) {
+        const int q = c + sy;
+        d13[c] = edge13<T, G>(p.geo, p.d1, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + 1], p.V1[q + 1], p.V1[q + 1 + sz]);
+    }
+    if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) {
+        const int q = c + 1;
+        d23[c] = edge23<T, G>(p.geo, p.d2, p.d3, i, j, p.V3[q + sz], p.V3[q + sz + sy], p.V2[q + sy], p.V2[q + sy + sz]);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // second invariant of τ at an interior cell s (compute_TII!, :246-255)
 template <typename T>
 __device__ __forceinline__ T tau_II(const KP<T>& p, int s) {

@@ -8,7 +8,11 @@
 #include <cuda_runtime.h>
 #include <cudaTypedefs.h>
 
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cerrno>
+#include <cstdarg>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -1212,6 +1216,37 @@ static int copy_field(Ctx* c, int32_t field, double* host, const double* src_hos
     return SPH_OK;
 }
 
+// one FP64 state slot with the extent e, in the reference's column-major layout
+static int copy_slot_out(Ctx* c, int slot, const int e[3], double* host) {
+    cudaMemcpy3DParms m;
+    std::memset(&m, 0, sizeof(m));
+    m.srcPtr = make_cudaPitchedPtr(c->s64.f[slot], sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
+    m.dstPtr = make_cudaPitchedPtr(host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
+    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
+    m.kind = cudaMemcpyDeviceToHost;
+    CK(cudaMemcpy3DAsync(&m, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+static std::string strf(const char* f, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, f);
+    std::vsnprintf(buf, sizeof(buf), f, ap);
+    va_end(ap);
+    return std::string(buf);
+}
+
+static int write_file(const std::string& path, const void* data, size_t bytes) {
+    FILE* f = std::fopen(path.c_str(), "wb");
+    if (!f) return fail(SPH_ERR_INVALID, "sph_save: cannot open " + path + " for writing");
+    const size_t w = bytes ? std::fwrite(data, 1, bytes, f) : 0;
+    const int cl = std::fclose(f);
+    if (w != bytes || cl != 0) return fail(SPH_ERR_INVALID, "sph_save: short write to " + path);
+    return SPH_OK;
+}
+
 int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
@@ -1338,6 +1373,91 @@ int sph_sweep(void* h, int64_t k) {
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_ms = ms;
     return check_kernel_flag(*c);
+}
+
+int sph_save(void* h, const char* dir, int32_t num, double tol, double runtime_s, const int64_t* hist_iter, const double* hist_err,
+             int64_t nhist) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !dir) return fail(SPH_ERR_INVALID, "sph_save: NULL argument");
+    if (nhist < 0 || (nhist > 0 && (!hist_iter || !hist_err))) return fail(SPH_ERR_INVALID, "sph_save: history");
+    int rc = sync64(*c);
+    if (rc) return rc;
+    if (mkdir(dir, 0777) != 0 && errno != EEXIST) return fail(SPH_ERR_INVALID, std::string("sph_save: cannot create ") + dir);
+    const std::string out = std::string(dir) + "/";
+    const sph_params& q = c->prm;
+    const int G = q.geometry;
+    // Save_infos: the scripts print εnonl and the run time with %d, which Julia's Printf
+    // renders for a Float64 as %.0f
+    std::string txt = strf("%d %f %f %f %d %d %d %.0f %.0f", num, q.l1, q.l2, q.l3, q.n1, q.n2, q.n3, tol, runtime_s);
+    if ((rc = write_file(out + std::to_string(num) + "_infos.inf", txt.data(), txt.size()))) return rc;
+    if (G == SPH_GEOM_SPHERICAL)
+        txt = strf("%d   %f  %f  %f    %f     %f   %f  %f, %f, %f, %f    , %f", num, q.eta0, q.rho0, q.rho_in, q.n_exp, q.tau_C, q.vr, q.g,
+                   q.sh, q.r, q.radius, q.dmp);
+    else if (G == SPH_GEOM_CYLINDRICAL)
+        txt = strf("%d  %f  %f  %f    %f     %f   %f  %f  %f  %f  %f      %f", num, q.eta0, q.rho0, q.rho_in, q.n_exp, q.tau_C, q.vr, q.g,
+                   q.sh, q.r, q.radius, q.dmp);
+    else
+        txt = strf("%d   %f  %f  %f    %f     %f   %f  %f  %f  %f      %f", num, q.eta0, q.rho0, q.rho_in, q.n_exp, q.tau_C, q.vr, q.g, q.sh,
+                   q.radius, q.dmp);
+    if ((rc = write_file(out + std::to_string(num) + "_phys.inf", txt.data(), txt.size()))) return rc;
+
+    auto save = [&](const char* name, const std::vector<double>& a) {
+        return write_file(out + "A_" + name + ".bin", a.data(), a.size() * sizeof(double));
+    };
+    auto save_field = [&](const char* name, int field) {
+        int e[3];
+        field_extent(c->d, field, e);
+        std::vector<double> a((size_t)e[0] * e[1] * e[2]);
+        int r = copy_field(c, field, a.data(), nullptr, (int64_t)a.size());
+        return r ? r : save(name, a);
+    };
+    const int n1 = q.n1, n2 = q.n2, n3 = q.n3;
+    const size_t nc = (size_t)n1 * n2 * n3;
+    // coordinate grids of the cell centres ([xc for xc = X_i, yc = Y_i, zc = Z_i])
+    std::vector<double> X(nc), Y(nc), Z(nc);
+    for (int k = 0; k < n3; ++k)
+        for (int j = 0; j < n2; ++j)
+            for (int i = 0; i < n1; ++i) {
+                const size_t t = i + (size_t)n1 * (j + (size_t)n2 * k);
+                X[t] = c->hx1[i]; Y[t] = c->hx2[j]; Z[t] = c->hx3[k];
+            }
+    static const char* const kSph[] = {"R", "TH", "PH", "VR", "VTH", "VPH", "TAU_RR", "TAU_THTH", "TAU_PHPH", "TAU_RTH", "TAU_RPH", "TAU_THPH"};
+    static const char* const kCyl[] = {"R", "TH", "Z", "VR", "VTH", "VZ", "TAU_RR", "TAU_THTH", "TAU_ZZ", "TAU_RTH", "TAU_RZ", "TAU_THZ"};
+    static const char* const kCart[] = {"X3D", "Y3D", "Z3D", "VX", "VY", "VZ", "TAU_XX", "TAU_YY", "TAU_ZZ", "TAU_XY", "TAU_XZ", "TAU_YZ"};
+    const char* const* nm = G == SPH_GEOM_SPHERICAL ? kSph : (G == SPH_GEOM_CYLINDRICAL ? kCyl : kCart);
+    if ((rc = save(nm[0], X)) || (rc = save(nm[1], Y)) || (rc = save(nm[2], Z))) return rc;
+    if ((rc = save_field("ETAS", SPH_FIELD_ETA)) || (rc = save_field("RHO", SPH_FIELD_RHO)) || (rc = save_field("P", SPH_FIELD_P))) return rc;
+    const int vf[9] = {SPH_FIELD_V1, SPH_FIELD_V2, SPH_FIELD_V3, SPH_FIELD_TAU11, SPH_FIELD_TAU22, SPH_FIELD_TAU33,
+                       SPH_FIELD_TAU12, SPH_FIELD_TAU13, SPH_FIELD_TAU23};
+    for (int i = 0; i < 9; ++i)
+        if ((rc = save_field(nm[3 + i], vf[i]))) return rc;
+    if ((rc = save_field("TII", SPH_FIELD_TII))) return rc;
+    if (G == SPH_GEOM_CYLINDRICAL) {
+        // ρG = ρ·g, DIVV and the strain rates D_* of the current velocities
+        std::vector<double> rho(nc);
+        if ((rc = copy_field(c, SPH_FIELD_RHO, rho.data(), nullptr, (int64_t)nc))) return rc;
+        for (double& v : rho) v *= q.g;
+        if ((rc = save("RHOG", rho))) return rc;
+        State<double>& st = c->s64;
+        KP<double> p = make_kp<double>(*c, st);
+        k_strain_out<double, CYL><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, st.f[F_SDD], st.f[F_Q11], st.f[F_Q22], st.f[F_Q33],
+                                                                                st.f[F_Q12], st.f[F_Q13], st.f[F_Q23]);
+        CK(cudaGetLastError());
+        static const char* const dn[7] = {"DIVV", "D_RR", "D_THTH", "D_ZZ", "D_RTH", "D_RZ", "D_THZ"};
+        const int ds[7] = {F_SDD, F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23};
+        const int df[7] = {SPH_FIELD_P, SPH_FIELD_P, SPH_FIELD_P, SPH_FIELD_P, SPH_FIELD_TAU12, SPH_FIELD_TAU13, SPH_FIELD_TAU23};
+        for (int i = 0; i < 7; ++i) {
+            int e[3];
+            field_extent(c->d, df[i], e);
+            std::vector<double> a((size_t)e[0] * e[1] * e[2]);
+            if ((rc = copy_slot_out(c, ds[i], e, a.data())) || (rc = save(dn[i], a))) return rc;
+        }
+    }
+    // err_evo / iter_evo: Data.Array(...) of the scripts, i.e. Float64
+    std::vector<double> ev((size_t)nhist), it((size_t)nhist);
+    for (int64_t i = 0; i < nhist; ++i) { ev[i] = hist_err[i]; it[i] = (double)hist_iter[i]; }
+    if ((rc = save("err_evo", ev)) || (rc = save("iter_evo", it))) return rc;
+    return SPH_OK;
 }
 
 int sph_sweep_profile(void* h, int64_t k, double* sweep_ms, double* kernel_ms) {

@@ -90,7 +90,9 @@ typedef enum sph_kernels { SPH_KERNELS_AUTO = 0, SPH_KERNELS_SIMPLE = 1 } sph_ke
 typedef enum sph_criterion {
     SPH_CRIT_REFERENCE = 0,  /* max_f max|V_f - V_f(previous iteration)| / max|V_f| < tol and iter > 20
                                 (SphericalStokes_diapir.jl:427-439) */
-    SPH_CRIT_RESIDUAL = 1    /* FP64 Stokes residual: max(max|R_mom|/f_scale, max|div V| l1/max|V|) < tol */
+    SPH_CRIT_RESIDUAL = 1,   /* FP64 Stokes residual: max(max|R_mom|/f_scale, max|div V| l1/max|V|) < tol */
+    SPH_CRIT_REFERENCE_PLATEAU = 2  /* SPH_CRIT_REFERENCE with the plateau script's rule: a NaN V3 ratio
+                                       (max|V3| = 0) is left out of the max (SphericalStokes_plateau.jl:540-552) */
 } sph_criterion;
 
 typedef enum sph_field {
@@ -194,6 +196,15 @@ int sph_set_stream(void* ctx, void* stream);
 /* copy a field from / to host memory in the reference layout (count = product of sph_field_dims) */
 int sph_set_field(void* ctx, int32_t field, const double* host, int64_t count);
 int sph_get_field(void* ctx, int32_t field, double* host, int64_t count);
+
+/* Changes the scalar parameters of a live context between solves (the continuation steps
+ * of SphericalStokes_plateau.jl:485-522 change vpdt through vr, and n_exp): vpdt (<= 0:
+ * from vr as in sph_create), dmp, l_ref, g, tau_C, n_exp, n_exp_late, switch_err, relax,
+ * edot_bg, r, sh, sig_bc, vr, eta0, etasm_passes.  geometry, precision, bc, rheology,
+ * kernels, n1..n3, c1..c3 and l1..l3 are fixed at sph_create (SPH_ERR_INVALID if they
+ * differ); init, rho0, rho_in, radius and incl_linear only act in sph_create.  Fields are
+ * kept; η and η_ini of a new step are set with sph_set_field. */
+int sph_update_params(void* ctx, const sph_params* params);
 
 /* exactly k reference PT iterations (equal3! ... BC_φ!, SphericalStokes_diapir.jl:413-425) */
 int sph_step(void* ctx, int64_t k);

@@ -546,8 +546,10 @@ void orc_sph_iterate(orc_sph_state* s, const orc_sph_params* q, int64_t niter) {
 }
 
 // check_err! + the reference's stopping norm  SphericalStokes_diapir.jl:332-344, 428-432:
-// max over the three velocity arrays of max|V - V_err| / max|V|
-double orc_sph_check_err(orc_sph_state* s) {
+// max over the three velocity arrays of max|V - V_err| / max|V|, NaN propagating as
+// Julia's maximum / max do.  skip_nan_phi: the plateau script's rule
+// (SphericalStokes_plateau.jl:540-552), a NaN Vφ ratio is left out.
+static double check_err_impl(orc_sph_state* s, bool skip_nan_phi) {
     const long nr = s->nr, nt = s->nt, np = s->np;
     long n[3] = {(nr + 1) * nt * np, nr * (nt + 1) * np, nr * nt * (np + 1)};
     double* V[3] = {s->VR, s->Vt, s->Vp};
@@ -560,10 +562,14 @@ double orc_sph_check_err(orc_sph_state* s) {
             md = nmax(md, E[f][c]);
             mv = nmax(mv, V[f][c]);
         }
-        err = std::max(err, md / mv);
+        const double r = md / mv;
+        if (r != r && skip_nan_phi && f == 2) continue;
+        err = (r != r || err != err) ? NAN : std::max(err, r);
     }
     return err;
 }
+double orc_sph_check_err(orc_sph_state* s) { return check_err_impl(s, false); }
+double orc_sph_check_err_plateau(orc_sph_state* s) { return check_err_impl(s, true); }
 
 // ---- EXT: FP64 Stokes residual ---------------------------------------------
 // Momentum residual at interior velocity nodes (the compute_V! increments with

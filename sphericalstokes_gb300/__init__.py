@@ -33,7 +33,7 @@ BC = {"diapir": 0, "free_slip": 1, "stress": 2}
 RHEO = {"linear": 0, "tau_power": 1, "tau_power_relax": 2, "edot_power_relax": 3}
 INIT = {"none": 0, "inclusion": 1}
 KERNELS_VARIANT = {"auto": 0, "simple": 1}
-CRIT = {"reference": 0, "residual": 1}
+CRIT = {"reference": 0, "residual": 1, "reference_plateau": 2}
 FIELDS = {
     "P": 0, "V1": 1, "V2": 2, "V3": 3, "TAU11": 4, "TAU22": 5, "TAU33": 6,
     "TAU12": 7, "TAU13": 8, "TAU23": 9, "ETA": 10, "ETA_INI": 11, "ETA_SM": 12,
@@ -97,6 +97,7 @@ _SIGS = {
     "sph_set_stream": ([C.c_void_p, C.c_void_p], C.c_int),
     "sph_set_field": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
     "sph_get_field": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
+    "sph_update_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
     "sph_step": ([C.c_void_p, C.c_int64], C.c_int),
     "sph_solve": ([C.c_void_p, C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.POINTER(C.c_int64),
                    C.POINTER(C.c_double), C.c_int64], C.c_int),
@@ -292,6 +293,11 @@ class Solver:
         return SolveResult(int(info.status), int(info.iters), int(info.outer), float(info.err), float(info.residual),
                            float(info.seconds), hi[:n].copy(), he[:n].copy(), float(info.device_ms), float(info.sweep_ms),
                            float(info.outer_ms))
+
+    def update_params(self, p: Params) -> None:
+        """Change scalar parameters between solves (``sph_update_params``); grid and model choices stay."""
+        _check(self.lib, self.lib.sph_update_params(self._h, C.byref(p)), "sph_update_params")
+        self.params = p
 
     def sweep(self, k: int) -> float:
         """k FP32 sweeps of the current defect-correction step (MIXED); returns their device time in ms."""

@@ -550,7 +550,7 @@ int fetch_red(Ctx& c) {
 
 // relative velocity change of the last iteration (the reference's err)
 template <typename T>
-int ref_err(Ctx& c, State<T>& s, double* err) {
+int ref_err(Ctx& c, State<T>& s, double* err, bool skip_nan_v3) {
     CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
     launch_maxabs<T>(c, s.f[F_V1], s.f[F_V1E], 0);
     launch_maxabs<T>(c, s.f[F_V2], s.f[F_V2E], 1);
@@ -565,6 +565,7 @@ int ref_err(Ctx& c, State<T>& s, double* err) {
     for (int f = 0; f < 3; ++f) {
         double dv = slot_val(c, f), vv = slot_val(c, 3 + f);
         double r = dv / vv;
+        if (!(r == r) && skip_nan_v3 && f == 2) continue;
         if (!(r == r)) { e = r; break; }
         e = std::max(e, r);
     }
@@ -652,18 +653,19 @@ int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_sol
     int64_t it = 0;
     double err = 1.0;
     int status = SPH_ERR_NOT_CONVERGED;
+    const bool ref = o.criterion == SPH_CRIT_REFERENCE || o.criterion == SPH_CRIT_REFERENCE_PLATEAU;
     while (it < o.maxiter) {
         ++it;
         const bool check = (it % nout) == 0;
-        if (check && o.criterion == SPH_CRIT_REFERENCE) {
+        if (check && ref) {
             int rc = snapshot<T>(c, s);
             if (rc) return rc;
         }
         iterate_dispatch<T>(c, s);
         if (!check) continue;
         CK(cudaGetLastError());
-        if (o.criterion == SPH_CRIT_REFERENCE) {
-            int rc = ref_err<T>(c, s, &err);
+        if (ref) {
+            int rc = ref_err<T>(c, s, &err, o.criterion == SPH_CRIT_REFERENCE_PLATEAU);
             if (rc) return rc;
         } else {
             if (is32) { c.stale64 = true; int rc = sync64(c); if (rc) return rc; }
@@ -679,7 +681,7 @@ int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_sol
         }
         if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
         if (c.prm.switch_err > 0.0 && err < c.prm.switch_err) c.cur_n = c.prm.n_exp_late;
-        if (err < o.tol && (o.criterion != SPH_CRIT_REFERENCE || it > 20)) { status = SPH_OK; break; }
+        if (err < o.tol && (!ref || it > 20)) { status = SPH_OK; break; }
     }
     if (info) { info->iters = it; info->err = err; info->status = status; }
     return SPH_OK;
@@ -931,7 +933,7 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
             if (check) { rc = snapshot<float>(c, t); if (rc) return rc; }
             iterate_dispatch<float>(c, t);
             if (!check) continue;
-            rc = ref_err<float>(c, t, &werr);
+            rc = ref_err<float>(c, t, &werr, false);
             if (rc) return rc;
             if (!(werr == werr)) return fail(SPH_ERR_DIVERGED, "NaN in the FP32 warm start");
             if (werr < o.warm_tol && iters > 20) break;
@@ -1148,6 +1150,35 @@ int sph_create(const sph_params* prm, void** out) {
     return SPH_OK;
 }
 
+int sph_update_params(void* h, const sph_params* p) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    int rc = check_params(p);
+    if (rc) return rc;
+    const sph_params& q = c->prm;
+    if (p->geometry != q.geometry || p->precision != q.precision || p->bc != q.bc || p->rheology != q.rheology ||
+        p->kernels != q.kernels || p->n1 != q.n1 || p->n2 != q.n2 || p->n3 != q.n3 || p->c1 != q.c1 || p->c2 != q.c2 ||
+        p->c3 != q.c3 || p->l1 != q.l1 || p->l2 != q.l2 || p->l3 != q.l3)
+        return fail(SPH_ERR_INVALID, "sph_update_params: geometry, precision, bc, rheology, kernels, n1..n3, c1..c3 and l1..l3 "
+                                     "are fixed at sph_create");
+    if ((rc = sync64(*c))) return rc;
+    sph_params n = *p;
+    if (n.vpdt <= 0.0) n.vpdt = n.l1 / (n.n1 - 1) * (1.0 / (2.0 + 4.5 * std::log10(n.vr)));
+    c->prm = n;
+    c->cur_n = n.n_exp;
+    // captured launches and the prepared correction problem hold the old scalars
+    for (int i = 0; i < 2; ++i) {
+        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
+        c->corr_graph[i] = nullptr;
+        c->corr_graph_key[i] = nullptr;
+    }
+    c->graph_len = 0;
+    c->corr_ready = false;
+    c->bc.clear();
+    if ((rc = build_bc(*c))) return rc;
+    return compute_f_scale(*c);
+}
+
 int sph_destroy(void* h) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return SPH_OK;
@@ -1292,6 +1323,7 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !o) return fail(SPH_ERR_INVALID, "NULL argument");
     if (o->tol <= 0.0 || o->maxiter <= 0) return fail(SPH_ERR_INVALID, "tol and maxiter must be positive");
+    if (o->criterion < SPH_CRIT_REFERENCE || o->criterion > SPH_CRIT_REFERENCE_PLATEAU) return fail(SPH_ERR_INVALID, "criterion");
     sph_solve_info local;
     std::memset(&local, 0, sizeof(local));
     sph_solve_info* inf = info ? info : &local;

@@ -296,6 +296,25 @@ def run_ours(args) -> None:
         if solve_info["mixed"]["converged"] and solve_info["fp64"]["converged"]:
             solve_info["speedup_mixed_vs_fp64"] = round(solve_info["fp64"]["seconds"] / solve_info["mixed"]["seconds"], 2)
 
+    batch_info = None
+    if args.batch > 0:
+        from sphericalstokes_gb300 import batch as B
+
+        edges = tuple(int(x) for x in args.batch_edges.split(","))
+        cases = B.sweep_cases(args.batch, seed=0, edges=edges)
+        bo = S.make_opts(tol=1e-8, maxiter=args.batch_budget, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=30,
+                         inner_max=args.batch_budget, warm_tol=1e-5)
+        rb = B.run(cases, bo, threads=args.batch_threads)
+        rs = B.run(cases, bo, serial=True)
+        conv = sum(1 for x in rb["results"] if x.converged)
+        batch_info = {"solves": args.batch, "edges": list(edges), "budget_sweeps": args.batch_budget,
+                      "solves_per_s": round(rb["solves_per_s"], 3), "serial_solves_per_s": round(rs["solves_per_s"], 3),
+                      "speedup_vs_serial": round(rs["wall_s"] / rb["wall_s"], 2), "converged": conv,
+                      "threads": args.batch_threads,
+                      "cases": "seed-0 draw: edge per axis from the list, geometry cycled sph/cyl/cart, n in 1..4, "
+                               "viscosity ratio log-U[1e-4,1e-1], stress ratio U[0,1]; mixed precision to residual 1e-8 "
+                               "or the sweep budget; autotuned chunk per size"}
+
     if rank != 0:
         return
     line = {
@@ -317,6 +336,8 @@ def run_ours(args) -> None:
         line["e2e"] = e2e
     if solve_info:
         line["time_to_tol"] = solve_info
+    if batch_info:
+        line["batch"] = batch_info
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(n, seconds=args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -341,7 +362,12 @@ def main():
     ap.add_argument("--max-outer", type=int, default=60)
     ap.add_argument("--inner-max", type=int, default=200_000)
     ap.add_argument("--warm-tol", type=float, default=1e-5)
-    ap.add_argument("--traffic", type=float, default=None, help="ncu DRAM bytes per sweep (from profiles/)")
+    ap.add_argument("--traffic", type=float, default=1.78e9,
+                    help="ncu DRAM bytes per launch of the fused sweep at 255^3 (profiles/k_fused_tma_sph255_traffic.md)")
+    ap.add_argument("--batch", type=int, default=12, help="batched-solve leg: number of solves (0: skip)")
+    ap.add_argument("--batch-edges", default="31,47", help="grid edges the batched solves draw from")
+    ap.add_argument("--batch-budget", type=int, default=20000, help="sweep budget per batched solve")
+    ap.add_argument("--batch-threads", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

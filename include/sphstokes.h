@@ -206,6 +206,21 @@ int sph_get_field(void* ctx, int32_t field, double* host, int64_t count);
  * kept; η and η_ini of a new step are set with sph_set_field. */
 int sph_update_params(void* ctx, const sph_params* params);
 
+/* Batch of independent solves (no counterpart in the reference, which solves one grid per
+ * script run): sph_solve of every context, contexts handed out to `threads` host threads
+ * (<= 0: one per host core), each context on its own CUDA stream, so many small grids
+ * share the GPU concurrently.  opts[i] and infos[i] belong to ctxs[i] (per-solve
+ * tolerance and iteration budget in, status out); no history is recorded.  A context
+ * may appear once.  Returns SPH_OK unless an argument or a CUDA call failed; the
+ * outcome of each solve is infos[i].status. */
+int sph_batch_solve(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph_solve_info* infos, int32_t threads);
+
+/* Autotuner of the fused FP32 sweep (no counterpart in the reference): times `sweeps`
+ * correction sweeps for each candidate x3 chunk length (planes per block) and keeps
+ * the fastest for this context and for every later context of the same geometry and
+ * grid size.  MIXED with SPH_KERNELS_AUTO only; the FP64 state is not changed. */
+int sph_autotune(void* ctx, int32_t sweeps, int32_t* best_chunk, double* best_ms_per_sweep);
+
 /* exactly k reference PT iterations (equal3! ... BC_φ!, SphericalStokes_diapir.jl:413-425) */
 int sph_step(void* ctx, int64_t k);
 

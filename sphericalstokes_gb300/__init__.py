@@ -98,6 +98,8 @@ _SIGS = {
     "sph_set_field": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
     "sph_get_field": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
     "sph_update_params": ([C.c_void_p, C.POINTER(Params)], C.c_int),
+    "sph_batch_solve": ([C.POINTER(C.c_void_p), C.c_int32, C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.c_int32], C.c_int),
+    "sph_autotune": ([C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)], C.c_int),
     "sph_step": ([C.c_void_p, C.c_int64], C.c_int),
     "sph_solve": ([C.c_void_p, C.POINTER(SolveOpts), C.POINTER(SolveInfo), C.POINTER(C.c_int64),
                    C.POINTER(C.c_double), C.c_int64], C.c_int),
@@ -294,6 +296,12 @@ class Solver:
                            float(info.seconds), hi[:n].copy(), he[:n].copy(), float(info.device_ms), float(info.sweep_ms),
                            float(info.outer_ms))
 
+    def autotune(self, sweeps: int = 20) -> tuple[int, float]:
+        """Pick the fused sweep's x3 chunk length for this grid size; returns (chunk, ms per sweep)."""
+        k, ms = C.c_int32(), C.c_double()
+        _check(self.lib, self.lib.sph_autotune(self._h, int(sweeps), C.byref(k), C.byref(ms)), "sph_autotune")
+        return int(k.value), float(ms.value)
+
     def update_params(self, p: Params) -> None:
         """Change scalar parameters between solves (``sph_update_params``); grid and model choices stay."""
         _check(self.lib, self.lib.sph_update_params(self._h, C.byref(p)), "sph_update_params")
@@ -355,3 +363,28 @@ def sector_params(n: int | tuple[int, int, int], **kw) -> Params:
                vpdt=hmin * cfl, init="inclusion")
     set_params(p, **kw)
     return p
+
+
+def make_opts(tol: float = 5e-7, maxiter: int = 100000, nout: int = 100, criterion: str = "reference",
+              inner_rtol: float = 1e-3, max_outer: int = 50, inner_max: int = 200000, warm_tol: float = 0.0) -> SolveOpts:
+    o = SolveOpts()
+    o.criterion = CRIT[criterion]
+    o.nout, o.maxiter, o.tol = nout, maxiter, tol
+    o.inner_rtol, o.max_outer, o.inner_max, o.warm_tol = inner_rtol, max_outer, inner_max, warm_tol
+    return o
+
+
+def solve_batch(solvers: list, opts: list | SolveOpts, threads: int = 0) -> list[SolveResult]:
+    """``sph_batch_solve``: every solver's PT solve, concurrently on the GPU (one stream each,
+    ``threads`` host threads); ``opts`` one SolveOpts for all or one per solver."""
+    lib = load_library()
+    n = len(solvers)
+    if isinstance(opts, SolveOpts):
+        opts = [opts] * n
+    ctxs = (C.c_void_p * n)(*[s._h for s in solvers])
+    oa = (SolveOpts * n)(*opts)
+    ia = (SolveInfo * n)()
+    _check(lib, lib.sph_batch_solve(ctxs, n, oa, ia, int(threads)), "sph_batch_solve")
+    empty_i, empty_e = np.zeros(0, dtype=np.int64), np.zeros(0)
+    return [SolveResult(int(x.status), int(x.iters), int(x.outer), float(x.err), float(x.residual), float(x.seconds),
+                        empty_i, empty_e, float(x.device_ms), float(x.sweep_ms), float(x.outer_ms)) for x in ia]

@@ -18,7 +18,11 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <map>
 #include <mutex>
+#include <thread>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -446,6 +450,10 @@ void swap_state(State<float>& s) {
     for (int i = 0; i < 10; ++i) std::swap(s.f[a[i]], s.f[b[i]]);
 }
 
+// x3 chunk lengths picked by sph_autotune, per (geometry, n1, n2, n3), shared by every context
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int>, int> g_tuned_chunk;
+
 int fused_chunk(const Ctx& c) {
     if (c.fused_chunk > 0) return c.fused_chunk;
     const long long xy = (long long)((c.d.n1 + FTX - 1) / FTX) * ((c.d.n2 + FTY - 1) / FTY);
@@ -735,16 +743,14 @@ int prepare_correction(Ctx& c, const double out[7]) {
 // ---------------------------------------------------------------------------
 // TMA tensor maps over the padded box of FP32 fields
 PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    static bool tried = false;
-    if (!tried) {
-        tried = true;
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {  // looked up once, thread-safe
         void* f = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    }
+            return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        return (PFN_cuTensorMapEncodeTiled_v12000) nullptr;
+    }();
     return fn;
 }
 
@@ -1115,6 +1121,11 @@ int sph_create(const sph_params* prm, void** out) {
     if (q.vpdt <= 0.0) q.vpdt = q.l1 / (q.n1 - 1) * (1.0 / (2.0 + 4.5 * std::log10(q.vr)));
     c->cur_n = q.n_exp;
     c->fused = q.kernels != SPH_KERNELS_SIMPLE;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        auto it = g_tuned_chunk.find(std::make_tuple(q.geometry, q.n1, q.n2, q.n3));
+        if (it != g_tuned_chunk.end()) c->fused_chunk = it->second;
+    }
     if (const char* e = std::getenv("SPH_FUSED_CHUNK")) c->fused_chunk = std::atoi(e);
     Dims& d = c->d;
     d.n1 = q.n1; d.n2 = q.n2; d.n3 = q.n3;
@@ -1147,6 +1158,89 @@ int sph_create(const sph_params* prm, void** out) {
     if ((rc = compute_f_scale(*c))) return cleanup(rc);
     c->stale32 = true;
     *out = c;
+    return SPH_OK;
+}
+
+int sph_batch_solve(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph_solve_info* infos, int32_t threads) {
+    if (n < 0 || (n > 0 && (!ctxs || !opts || !infos))) return fail(SPH_ERR_INVALID, "sph_batch_solve: NULL argument");
+    for (int32_t i = 0; i < n; ++i) {
+        if (!ctxs[i]) return fail(SPH_ERR_INVALID, "sph_batch_solve: NULL context");
+        for (int32_t j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(SPH_ERR_INVALID, "sph_batch_solve: a context appears twice");
+    }
+    if (n == 0) return SPH_OK;
+    int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
+    nt = std::max(1, std::min(nt, (int)n));
+    int dev = 0;
+    CK(cudaGetDevice(&dev));
+    std::atomic<int32_t> next(0);
+    std::vector<std::string> errs(n);
+    auto worker = [&]() {
+        cudaSetDevice(dev);  // the caller's device in every worker
+        for (int32_t i = next.fetch_add(1); i < n; i = next.fetch_add(1)) {
+            const int rc = sph_solve(ctxs[i], &opts[i], &infos[i], nullptr, nullptr, 0);
+            if (rc != SPH_OK && rc != SPH_ERR_NOT_CONVERGED && rc != SPH_ERR_DIVERGED) {
+                infos[i].status = rc;
+                errs[i] = g_err;
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(worker);
+    worker();
+    for (auto& t : pool) t.join();
+    for (int32_t i = 0; i < n; ++i)
+        if (!errs[i].empty()) return fail(infos[i].status, "solve " + std::to_string(i) + ": " + errs[i]);
+    return SPH_OK;
+}
+
+int sph_autotune(void* h, int32_t sweeps, int32_t* best_chunk, double* best_ms) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (c->prm.precision != SPH_PREC_MIXED || !c->fused) return fail(SPH_ERR_UNSUPPORTED, "sph_autotune tunes the fused FP32 sweep (MIXED, SPH_KERNELS_AUTO)");
+    if (sweeps < 2) sweeps = 2;
+    int rc = sph_sweep(h, 0);  // prepares a correction problem (FP64 state unchanged)
+    if (rc) return rc;
+    const int G = c->prm.geometry;
+    const int n3 = c->d.n3;
+    const int cand[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192, 256};
+    struct Restore {
+        Ctx* c;
+        bool graphs;
+        ~Restore() { c->use_graphs = graphs; c->corr_ready = false; }
+    } restore{c, c->use_graphs};
+    c->use_graphs = false;
+    double bms = 1e300;
+    int bk = 0;
+    for (int kc : cand) {
+        if (kc > n3 && bk) break;
+        c->fused_chunk = std::min(kc, n3);
+        rc = G == SPH ? run_correction_sweeps<SPH>(*c, 1) : (G == CYL ? run_correction_sweeps<CYL>(*c, 1) : run_correction_sweeps<CART>(*c, 1));
+        if (rc) return rc;
+        CK(cudaEventRecord(c->ev0, c->stream));
+        rc = G == SPH ? run_correction_sweeps<SPH>(*c, sweeps) : (G == CYL ? run_correction_sweeps<CYL>(*c, sweeps) : run_correction_sweeps<CART>(*c, sweeps));
+        if (rc) return rc;
+        CK(cudaEventRecord(c->ev1, c->stream));
+        CK(cudaEventSynchronize(c->ev1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        if (ms < bms) { bms = ms; bk = c->fused_chunk; }
+        if (kc >= n3) break;
+    }
+    if ((rc = check_kernel_flag(*c))) return rc;
+    c->fused_chunk = bk;
+    for (int i = 0; i < 2; ++i) {  // graphs were captured with the previous chunk length
+        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
+        c->corr_graph[i] = nullptr;
+        c->corr_graph_key[i] = nullptr;
+    }
+    c->graph_len = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mu);
+        g_tuned_chunk[std::make_tuple(c->prm.geometry, c->d.n1, c->d.n2, c->d.n3)] = bk;
+    }
+    if (best_chunk) *best_chunk = bk;
+    if (best_ms) *best_ms = bms / sweeps;
     return SPH_OK;
 }
 

@@ -1,0 +1,84 @@
+"""Batched solves: the case generator (CPU) and, on the GPU, sph_batch_solve against the
+same solves run one after another, and the autotuner's chunk choice against results."""
+import numpy as np
+import pytest
+
+import sphericalstokes_gb300 as S
+from sphericalstokes_gb300 import batch as B
+
+FIELDS = ("P", "V1", "V2", "V3", "TAU11", "TAU12", "TAU13", "TAU23", "ETA")
+
+
+def test_sweep_cases_follow_the_distribution():
+    cases = B.sweep_cases(256, seed=0)
+    assert len(cases) == 256
+    assert [c.geometry for c in cases[:6]] == [0, 1, 2, 0, 1, 2]
+    assert all(c.n1 in B.EDGES and c.n2 in B.EDGES and c.n3 in B.EDGES for c in cases)
+    ns = [c.n_exp if c.rheology == S.RHEO["edot_power_relax"] else 1.0 for c in cases]
+    assert set(ns) == {1.0, 2.0, 3.0, 4.0}
+    ratios = np.array([1.0 / c.vr for c in cases])
+    assert ratios.min() >= 1e-4 and ratios.max() <= 1e-1
+    again = B.sweep_cases(256, seed=0)
+    assert all(a.n1 == b.n1 and a.vr == b.vr and a.sig_bc[1] == b.sig_bc[1] and a.sh == b.sh for a, b in zip(cases, again))
+
+
+def _small_cases(precision):
+    return [
+        S.sector_params((23, 17, 15), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                        sig_bc=(0.0, 0.5, -0.5), incl_linear=1, precision=precision),
+        S.default_params("cylindrical", n1=19, n2=15, n3=13, rheology="linear", bc="stress", sig_bc=(0.0, 0.3, -0.3),
+                         incl_linear=1, precision=precision),
+        S.default_params("cartesian", n1=17, n2=15, n3=19, rheology="linear", incl_linear=1, precision=precision),
+        S.sector_params((31, 15, 21), bc="free_slip", rheology="linear", precision=precision),
+    ]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision,crit", [("fp64", "reference"), ("mixed", "residual")])
+def test_batch_equals_serial(precision, crit):
+    """every solve of the batch computes exactly what it computes alone (own stream, deterministic kernels)"""
+    cases = _small_cases(precision)
+    if crit == "reference":
+        opts = S.make_opts(tol=1e-30, maxiter=400, nout=100, criterion=crit)
+    else:
+        opts = S.make_opts(tol=1e-8, maxiter=20000, nout=100, criterion=crit, inner_rtol=1e-2, max_outer=4, inner_max=4000)
+    serial, fields_s = [], []
+    for p in cases:
+        with S.Solver(p) as sv:
+            serial.append(sv.solve(tol=opts.tol, maxiter=opts.maxiter, nout=opts.nout, criterion=crit, inner_rtol=opts.inner_rtol,
+                                   max_outer=opts.max_outer, inner_max=opts.inner_max))
+            fields_s.append({f: sv.get(f) for f in FIELDS})
+    solvers = [S.Solver(p) for p in _small_cases(precision)]
+    try:
+        res = S.solve_batch(solvers, opts, threads=3)
+        fields_b = [{f: sv.get(f) for f in FIELDS} for sv in solvers]
+    finally:
+        for sv in solvers:
+            sv.close()
+    for i, (a, b) in enumerate(zip(serial, res)):
+        assert (a.status, a.iters, a.outer) == (b.status, b.iters, b.outer), i
+        for f in FIELDS:
+            np.testing.assert_array_equal(fields_b[i][f], fields_s[i][f], err_msg=f"case {i} {f}")
+
+
+@pytest.mark.gpu
+def test_autotuned_chunk_gives_the_same_sweeps():
+    p = _small_cases("mixed")[0]
+    out = []
+    for tune in (False, True):
+        with S.Solver(p) as sv:
+            if tune:
+                k, ms = sv.autotune(sweeps=6)
+                assert 1 <= k <= p.n3 and ms > 0.0
+            sv.sweep(57)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
+    for f in out[0]:
+        np.testing.assert_array_equal(out[1][f], out[0][f], err_msg=f)
+
+
+@pytest.mark.gpu
+def test_batch_rejects_a_context_twice():
+    with S.Solver(_small_cases("fp64")[3]) as sv:
+        with pytest.raises(S.SphError):
+            S.solve_batch([sv, sv], S.make_opts(maxiter=10), threads=2)

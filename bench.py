@@ -199,6 +199,35 @@ def run_reference(args) -> None:
 
 
 # ---------------------------------------------------------------------------
+# replicas: every rank solves its own copy of the workload on its own GPU; the only
+# communication is the barrier around the timed region and the max of the per-rank times
+def replica_group(world: int):
+    """The process group of the replicas (gloo on host memory), or None for one process."""
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+
+    if not dist.is_initialized():
+        dist.init_process_group("gloo")
+    return dist
+
+
+def replica_barrier(dist) -> None:
+    if dist is not None:
+        dist.barrier()
+
+
+def replica_max(dist, x: float) -> float:
+    """Max of x over the replicas (the slowest rank's time)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_ours(args) -> None:
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -208,25 +237,13 @@ def run_ours(args) -> None:
 
     import sphericalstokes_gb300 as S
 
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        dist.init_process_group("gloo")
+    dist = replica_group(world)
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        replica_barrier(dist)
 
     def max_over_ranks(x: float) -> float:
-        if dist is None:
-            return x
-        import torch
-
-        t = torch.tensor([x], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return replica_max(dist, x)
 
     n = args.n
     word = 4

@@ -243,6 +243,32 @@ int sph_sweep_apply(void* ctx);
  * launches.  Needs SPH_KERNELS_AUTO. */
 int sph_sweep_profile(void* ctx, int64_t k, double* sweep_ms, double* kernel_ms);
 
+/* Residual fields of the current state (FP64, the SPH_CRIT_RESIDUAL definition before the
+ * norms), in the reference layout: rV1..rV3 with the velocity arrays' sizes (non-zero at
+ * interior nodes only), rP = div V with the pressure array's size.  NULL skips a field.
+ * (No counterpart in the reference, which monitors only the velocity change.) */
+int sph_residual_fields(void* ctx, double* rV1, double* rV2, double* rV3, double* rP);
+
+/* Adjoint of the residual with the viscosity frozen at its current value (the linear
+ * operator of one Picard step; for the strain-rate law, η is the law's value at the current
+ * V and its dependence on V is not differentiated).  No counterpart in the reference.
+ * In: λ for the residual rows (lV1..lV3 velocity-array sizes, lP pressure size; NULL = 0).
+ * Out (NULL skips): aV1..aV3, aP = (∂R/∂(V,P))ᵀ λ; g_eta = (∂R/∂η)ᵀ λ and g_rho = (∂R/∂ρ)ᵀ λ
+ * per cell.  flags bit 0: compose with the transposed homogeneous BC program, i.e. the
+ * derivative with respect to the interior velocities (boundary entries come out zero);
+ * without it every velocity entry is an independent input. */
+int sph_residual_vjp(void* ctx, const double* lV1, const double* lV2, const double* lV3, const double* lP, double* aV1,
+                     double* aV2, double* aV3, double* aP, double* g_eta, double* g_rho, int32_t flags);
+
+/* Transposed PT solve (no counterpart in the reference): λ with Aᵀ λ = b, A the residual's
+ * Jacobian in the interior-unknown form of sph_residual_vjp, iterated on the device with the
+ * forward scheme's pseudo-steps (DT_R for the velocity rows, KBDT for the pressure rows).
+ * b and λ in the layouts of sph_residual_vjp; λ holds the initial guess on entry.  Stops when
+ * max|Aᵀλ - b| <= opts->tol * max|b| (checked every opts->nout iterations) or after
+ * opts->maxiter.  Returns the solve status (SPH_OK, SPH_ERR_NOT_CONVERGED, SPH_ERR_DIVERGED). */
+int sph_adjoint_solve(void* ctx, const double* bV1, const double* bV2, const double* bV3, const double* bP, double* lV1,
+                      double* lV2, double* lV3, double* lP, const sph_solve_opts* opts, sph_solve_info* info);
+
 /* Writes the results in the scripts' output format (Save_infos, Save_phys, SaveArray,
  * SphericalStokes_diapir.jl:23-43, :461-485; CylindricalStokes_diapir.jl:18-37, :390-419;
  * CartesianStokes_diapir.jl:18-37, :404-425) into the directory `dir` (created if absent):

@@ -30,6 +30,7 @@
 #include "sph_pt.cuh"
 #include "sph_fused.cuh"
 #include "sph_sweep_x2.cuh"
+#include "sph_adjoint.cuh"
 #include "sphstokes.h"
 
 using namespace sph;
@@ -107,6 +108,7 @@ struct Ctx {
     bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep
+    double* adj = nullptr;  // adjoint arrays (AJ_COUNT slots of the box), allocated on first use
     // per-launch timing of the fused sweep kernel (sph_sweep_profile): event pairs
     // recorded around each launch while prof_next < prof_ev.size()/2
     std::vector<cudaEvent_t> prof_ev;
@@ -1292,6 +1294,7 @@ int sph_destroy(void* h) {
     if (c->ev3) cudaEventDestroy(c->ev3);
     if (c->ev4) cudaEventDestroy(c->ev4);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+    if (c->adj) cudaFree(c->adj);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SPH_OK;
@@ -1371,6 +1374,154 @@ static int write_file(const std::string& path, const void* data, size_t bytes) {
     if (w != bytes || cl != 0) return fail(SPH_ERR_INVALID, "sph_save: short write to " + path);
     return SPH_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// adjoint of the FP64 residual (sph_adjoint.cuh)
+enum AdjSlot {
+    AJ_LV1, AJ_LV2, AJ_LV3, AJ_LP, AJ_S11, AJ_S22, AJ_S33, AJ_T12, AJ_T13, AJ_T23,
+    AJ_V1, AJ_V2, AJ_V3, AJ_P, AJ_GETA, AJ_GRHO, AJ_B1, AJ_B2, AJ_B3, AJ_BP, AJ_R1, AJ_R2, AJ_R3, AJ_RP, AJ_ETA, AJ_COUNT
+};
+
+static int adj_alloc(Ctx* c) {
+    if (c->adj) return SPH_OK;
+    const size_t b = sizeof(double) * (size_t)c->d.vol * AJ_COUNT;
+    if (cudaMalloc((void**)&c->adj, b) != cudaSuccess) return fail(SPH_ERR_NOMEM, "adjoint arrays");
+    CK(cudaMemsetAsync(c->adj, 0, b, c->stream));
+    return SPH_OK;
+}
+static double* adj_slot(Ctx* c, int s) { return c->adj + (size_t)s * c->d.vol; }
+
+// host array with a field's extent (reference layout) <-> an adjoint slot; NULL host: zero
+static int adj_upload(Ctx* c, int slot, int field, const double* host) {
+    double* dev = adj_slot(c, slot);
+    CK(cudaMemsetAsync(dev, 0, sizeof(double) * c->d.vol, c->stream));
+    if (!host) return SPH_OK;
+    int e[3];
+    field_extent(c->d, field, e);
+    cudaMemcpy3DParms m;
+    std::memset(&m, 0, sizeof(m));
+    m.srcPtr = make_cudaPitchedPtr(const_cast<double*>(host), sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
+    m.dstPtr = make_cudaPitchedPtr(dev, sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
+    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
+    m.kind = cudaMemcpyHostToDevice;
+    CK(cudaMemcpy3DAsync(&m, c->stream));
+    return SPH_OK;
+}
+static int adj_download(Ctx* c, int slot, int field, double* host) {
+    if (!host) return SPH_OK;
+    int e[3];
+    field_extent(c->d, field, e);
+    cudaMemcpy3DParms m;
+    std::memset(&m, 0, sizeof(m));
+    m.srcPtr = make_cudaPitchedPtr(adj_slot(c, slot), sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
+    m.dstPtr = make_cudaPitchedPtr(host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
+    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
+    m.kind = cudaMemcpyDeviceToHost;
+    CK(cudaMemcpy3DAsync(&m, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+// KP of the adjoint: the FP64 state with η = the residual's viscosity (the law's target for
+// the strain-rate law, frozen at the current V), ηSM and DT_R recomputed from it
+template <int G>
+static KP<double> adj_kp(Ctx* c) {
+    State<double>& s = c->s64;
+    KP<double> p = make_kp<double>(*c, s);
+    double* eta = adj_slot(c, AJ_ETA);
+    if (c->prm.rheology == SPH_RHEO_EDOT_POWER_RELAX) {
+        k_strain<double, G><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+        k_edot_law<double, false><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+        cudaMemcpyAsync(eta, s.f[F_ETA_OUT], sizeof(double) * c->d.vol, cudaMemcpyDeviceToDevice, c->stream);
+    } else {
+        cudaMemcpyAsync(eta, s.f[F_ETA], sizeof(double) * c->d.vol, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    p.eta = eta;
+    KP<double> q = p;
+    q.etaSM = s.f[F_ETA_SM];
+    k_maxloc<double><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(q, G == CART);
+    k_pt_dtr<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p);
+    return p;
+}
+
+static Adj adj_ptrs(Ctx* c) {
+    Adj a;
+    a.lV1 = adj_slot(c, AJ_LV1); a.lV2 = adj_slot(c, AJ_LV2); a.lV3 = adj_slot(c, AJ_LV3); a.lP = adj_slot(c, AJ_LP);
+    a.aS11 = adj_slot(c, AJ_S11); a.aS22 = adj_slot(c, AJ_S22); a.aS33 = adj_slot(c, AJ_S33);
+    a.aT12 = adj_slot(c, AJ_T12); a.aT13 = adj_slot(c, AJ_T13); a.aT23 = adj_slot(c, AJ_T23);
+    a.aV1 = adj_slot(c, AJ_V1); a.aV2 = adj_slot(c, AJ_V2); a.aV3 = adj_slot(c, AJ_V3); a.aP = adj_slot(c, AJ_P);
+    a.gEta = adj_slot(c, AJ_GETA); a.gRho = adj_slot(c, AJ_GRHO);
+    return a;
+}
+
+// Aᵀ λ (λ in the AJ_L* slots) into AJ_V*, AJ_P, with ∂R/∂η, ∂R/∂ρ contractions; with_bc: the
+// transposed homogeneous BC program (interior-unknown form)
+template <int G>
+static int adj_apply(Ctx* c, KP<double>& p, bool with_bc) {
+    Adj a = adj_ptrs(c);
+    CK(cudaMemsetAsync(adj_slot(c, AJ_S11), 0, sizeof(double) * c->d.vol * (AJ_GRHO - AJ_S11 + 1), c->stream));
+    k_vjp_momentum<G><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p, a);
+    k_vjp_pressure<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);
+    k_vjp_strain<G><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);
+    if (with_bc) {
+        KP<double> hp = p;
+        hp.sig2 = 0.0; hp.sig3 = 0.0;
+        for (auto it = c->bc.rbegin(); it != c->bc.rend(); ++it) {
+            const BcStage& st = *it;
+            int eu = st.dim == 0 ? c->d.n2 + 1 : c->d.n1 + 1;
+            int ev = st.dim == 2 ? c->d.n2 + 1 : c->d.n3 + 1;
+            dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
+            k_bc_adjoint<G><<<g, blk2d(), 0, c->stream>>>(hp, a, st);
+        }
+    }
+    CK(cudaGetLastError());
+    return SPH_OK;
+}
+
+template <int G>
+static int adjoint_solve_g(Ctx* c, const sph_solve_opts& o, sph_solve_info* inf) {
+    KP<double> p = adj_kp<G>(c);
+    Adj a = adj_ptrs(c);
+    const int nout = o.nout > 0 ? o.nout : 100;
+    // max|b|
+    CK(cudaMemsetAsync(c->red, 0, sizeof(unsigned long long) * kRedSlots, c->stream));
+    for (int s = 0; s < 4; ++s) launch_maxabs<double>(*c, adj_slot(c, AJ_B1 + s), nullptr, s);
+    int rc = fetch_red(*c);
+    if (rc) return rc;
+    double bmax = 0.0;
+    for (int s = 0; s < 4; ++s) bmax = std::max(bmax, slot_val(*c, s));
+    if (bmax == 0.0) bmax = 1.0;
+    dim3 gu((c->d.n1 + 1 + 31) / 32, (c->d.n2 + 1 + 7) / 8, c->d.n3 + 1);
+    int64_t it = 0;
+    double err = 1.0;
+    int status = SPH_ERR_NOT_CONVERGED;
+    while (it < o.maxiter) {
+        ++it;
+        if ((rc = adj_apply<G>(c, p, true))) return rc;
+        k_adjoint_update<<<gu, blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_LV1), adj_slot(c, AJ_LV2), adj_slot(c, AJ_LV3),
+                                                        adj_slot(c, AJ_LP), adj_slot(c, AJ_B1), adj_slot(c, AJ_B2), adj_slot(c, AJ_B3),
+                                                        adj_slot(c, AJ_BP), adj_slot(c, AJ_R1), adj_slot(c, AJ_R2), adj_slot(c, AJ_R3),
+                                                        adj_slot(c, AJ_RP));
+        if (it % nout) continue;
+        CK(cudaMemsetAsync(c->red, 0, sizeof(unsigned long long) * kRedSlots, c->stream));
+        for (int s = 0; s < 4; ++s) launch_maxabs<double>(*c, adj_slot(c, AJ_R1 + s), nullptr, s);
+        if ((rc = fetch_red(*c))) return rc;
+        double r = 0.0;
+        for (int s = 0; s < 4; ++s) r = std::max(r, slot_val(*c, s));
+        err = r / bmax;
+        if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
+        if (err < o.tol) { status = SPH_OK; break; }
+    }
+    inf->iters = it;
+    inf->err = err;
+    inf->residual = err;
+    inf->status = status;
+    return SPH_OK;
+}
+
+extern "C" {
 
 int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
     Ctx* c = static_cast<Ctx*>(h);
@@ -1499,6 +1650,76 @@ int sph_sweep(void* h, int64_t k) {
     CK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
     c->last_ms = ms;
     return check_kernel_flag(*c);
+}
+
+int sph_residual_fields(void* h, double* rV1, double* rV2, double* rV3, double* rP) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    int rc = sync64(*c);
+    if (rc) return rc;
+    double out[7];
+    if ((rc = residual64(*c, out))) return rc;
+    const int slots[4] = {F_RV1, F_RV2, F_RV3, F_RP};
+    const int fields[4] = {SPH_FIELD_V1, SPH_FIELD_V2, SPH_FIELD_V3, SPH_FIELD_P};
+    double* hs[4] = {rV1, rV2, rV3, rP};
+    for (int i = 0; i < 4; ++i) {
+        if (!hs[i]) continue;
+        int e[3];
+        field_extent(c->d, fields[i], e);
+        if ((rc = copy_slot_out(c, slots[i], e, hs[i]))) return rc;
+    }
+    return SPH_OK;
+}
+
+int sph_residual_vjp(void* h, const double* lV1, const double* lV2, const double* lV3, const double* lP, double* aV1, double* aV2,
+                     double* aV3, double* aP, double* g_eta, double* g_rho, int32_t flags) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    int rc = sync64(*c);
+    if (rc || (rc = adj_alloc(c))) return rc;
+    if ((rc = adj_upload(c, AJ_LV1, SPH_FIELD_V1, lV1)) || (rc = adj_upload(c, AJ_LV2, SPH_FIELD_V2, lV2)) ||
+        (rc = adj_upload(c, AJ_LV3, SPH_FIELD_V3, lV3)) || (rc = adj_upload(c, AJ_LP, SPH_FIELD_P, lP)))
+        return rc;
+    const int G = c->prm.geometry;
+    const bool bc = (flags & 1) != 0;
+    if (G == SPH) { KP<double> p = adj_kp<SPH>(c); rc = adj_apply<SPH>(c, p, bc); }
+    else if (G == CYL) { KP<double> p = adj_kp<CYL>(c); rc = adj_apply<CYL>(c, p, bc); }
+    else { KP<double> p = adj_kp<CART>(c); rc = adj_apply<CART>(c, p, bc); }
+    if (rc) return rc;
+    if ((rc = adj_download(c, AJ_V1, SPH_FIELD_V1, aV1)) || (rc = adj_download(c, AJ_V2, SPH_FIELD_V2, aV2)) ||
+        (rc = adj_download(c, AJ_V3, SPH_FIELD_V3, aV3)) || (rc = adj_download(c, AJ_P, SPH_FIELD_P, aP)) ||
+        (rc = adj_download(c, AJ_GETA, SPH_FIELD_P, g_eta)) || (rc = adj_download(c, AJ_GRHO, SPH_FIELD_P, g_rho)))
+        return rc;
+    CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_adjoint_solve(void* h, const double* bV1, const double* bV2, const double* bV3, const double* bP, double* lV1, double* lV2,
+                      double* lV3, double* lP, const sph_solve_opts* o, sph_solve_info* info) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !o || !lV1 || !lV2 || !lV3 || !lP) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (o->tol <= 0.0 || o->maxiter <= 0) return fail(SPH_ERR_INVALID, "tol and maxiter must be positive");
+    int rc = sync64(*c);
+    if (rc || (rc = adj_alloc(c))) return rc;
+    if ((rc = adj_upload(c, AJ_B1, SPH_FIELD_V1, bV1)) || (rc = adj_upload(c, AJ_B2, SPH_FIELD_V2, bV2)) ||
+        (rc = adj_upload(c, AJ_B3, SPH_FIELD_V3, bV3)) || (rc = adj_upload(c, AJ_BP, SPH_FIELD_P, bP)) ||
+        (rc = adj_upload(c, AJ_LV1, SPH_FIELD_V1, lV1)) || (rc = adj_upload(c, AJ_LV2, SPH_FIELD_V2, lV2)) ||
+        (rc = adj_upload(c, AJ_LV3, SPH_FIELD_V3, lV3)) || (rc = adj_upload(c, AJ_LP, SPH_FIELD_P, lP)))
+        return rc;
+    for (int s = AJ_R1; s <= AJ_RP; ++s) CK(cudaMemsetAsync(adj_slot(c, s), 0, sizeof(double) * c->d.vol, c->stream));
+    sph_solve_info local;
+    std::memset(&local, 0, sizeof(local));
+    sph_solve_info* inf = info ? info : &local;
+    std::memset(inf, 0, sizeof(*inf));
+    auto t0 = std::chrono::steady_clock::now();
+    const int G = c->prm.geometry;
+    rc = G == SPH ? adjoint_solve_g<SPH>(c, *o, inf) : (G == CYL ? adjoint_solve_g<CYL>(c, *o, inf) : adjoint_solve_g<CART>(c, *o, inf));
+    if (rc) return rc;
+    inf->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if ((rc = adj_download(c, AJ_LV1, SPH_FIELD_V1, lV1)) || (rc = adj_download(c, AJ_LV2, SPH_FIELD_V2, lV2)) ||
+        (rc = adj_download(c, AJ_LV3, SPH_FIELD_V3, lV3)) || (rc = adj_download(c, AJ_LP, SPH_FIELD_P, lP)))
+        return rc;
+    return inf->status;
 }
 
 int sph_save(void* h, const char* dir, int32_t num, double tol, double runtime_s, const int64_t* hist_iter, const double* hist_err,

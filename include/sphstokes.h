@@ -249,9 +249,8 @@ int sph_sweep_profile(void* ctx, int64_t k, double* sweep_ms, double* kernel_ms)
  * (No counterpart in the reference, which monitors only the velocity change.) */
 int sph_residual_fields(void* ctx, double* rV1, double* rV2, double* rV3, double* rP);
 
-/* Adjoint of the residual with the viscosity frozen at its current value (the linear
- * operator of one Picard step; for the strain-rate law, η is the law's value at the current
- * V and its dependence on V is not differentiated).  No counterpart in the reference.
+/* Adjoint of the residual (no counterpart in the reference): linear rheology exactly; for the
+ * strain-rate law the full Jacobian, η's dependence on V included (sph_residual_vjp_law).
  * In: λ for the residual rows (lV1..lV3 velocity-array sizes, lP pressure size; NULL = 0).
  * Out (NULL skips): aV1..aV3, aP = (∂R/∂(V,P))ᵀ λ; g_eta = (∂R/∂η)ᵀ λ and g_rho = (∂R/∂ρ)ᵀ λ
  * per cell.  flags bit 0: compose with the transposed homogeneous BC program, i.e. the
@@ -259,6 +258,13 @@ int sph_residual_fields(void* ctx, double* rV1, double* rV2, double* rV3, double
  * without it every velocity entry is an independent input. */
 int sph_residual_vjp(void* ctx, const double* lV1, const double* lV2, const double* lV3, const double* lP, double* aV1,
                      double* aV2, double* aV3, double* aP, double* g_eta, double* g_rho, int32_t flags);
+
+/* After sph_residual_vjp: its η contraction carried through the viscosity law, per cell
+ * g_eta_ini = (∂R/∂η_ini)ᵀ λ and the total g_n = (∂R/∂n)ᵀ λ (strain-rate law, unrelaxed target
+ * η_t; phase cells and the linear rheology: η = η_ini, g_n = 0).  NULL skips an output.  For
+ * the strain-rate law sph_residual_vjp and sph_adjoint_solve include the law's dependence on
+ * V (the Jacobian of the residual as the forward solver defines it). */
+int sph_residual_vjp_law(void* ctx, double* g_eta_ini, double* g_n);
 
 /* Transposed PT solve (no counterpart in the reference): λ with Aᵀ λ = b, A the residual's
  * Jacobian in the interior-unknown form of sph_residual_vjp, iterated on the device with the

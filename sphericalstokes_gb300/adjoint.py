@@ -8,9 +8,10 @@ With R(u; η, ρ) = 0 the discrete Stokes equations of the current state
 
 ``sph_residual_vjp`` applies (∂R/∂u)ᵀ and the two contractions with the
 hand-written transposed stencils; ``sph_adjoint_solve`` solves for λ with the
-forward PT scheme's pseudo-steps on the transposed rows.  The viscosity is
-frozen at its current value (exact for the linear rheology; for a power law the
-linear operator of one Picard step).
+forward PT scheme's pseudo-steps on the transposed rows.  For the linear
+rheology the viscosity is the parameter; for the strain-rate power law the
+Jacobian includes η's dependence on V and the gradients are with respect to the
+per-cell prefactor η_ini and the exponent n (``law_vjp``).
 """
 from __future__ import annotations
 
@@ -55,6 +56,15 @@ def vjp(sv: Solver, lam: dict, interior: bool = True) -> dict:
     return out
 
 
+def law_vjp(sv: Solver) -> tuple[np.ndarray, float]:
+    """After :func:`vjp`: its η contraction through the viscosity law — per cell (∂R/∂η_ini)ᵀλ
+    and the total (∂R/∂n)ᵀλ (``sph_residual_vjp_law``)."""
+    g = _empty(sv, "P")
+    gn = C.c_double()
+    _check(sv.lib, sv.lib.sph_residual_vjp_law(sv._h, _ptr(g), C.byref(gn)), "sph_residual_vjp_law")
+    return g, float(gn.value)
+
+
 def adjoint_solve(sv: Solver, b: dict, tol: float = 1e-10, maxiter: int = 1_000_000, nout: int = 500, lam0: dict | None = None):
     """λ with (∂R/∂u)ᵀ λ = b (interior-unknown form); returns (λ, SolveInfo)."""
     bs = [_fortran(b.get(f)) for f in VEL + ("P",)]
@@ -85,5 +95,7 @@ def gradient(sv: Solver, objective=surface_misfit, tol: float = 1e-10, maxiter: 
     J, b = objective(sv)
     lam, info = adjoint_solve(sv, b, tol=tol, maxiter=maxiter)
     g = vjp(sv, lam, interior=True)
-    eta = sv.get("ETA")
-    return {"J": J, "dlogeta": -eta * g["ETA"], "drho": -g["RHO"], "lambda": lam, "info": info}
+    g_ini, g_n = law_vjp(sv)
+    eta, eta_ini = sv.get("ETA"), sv.get("ETA_INI")
+    return {"J": J, "dlogeta": -eta * g["ETA"], "dlogeta_ini": -eta_ini * g_ini, "dn": -g_n, "drho": -g["RHO"],
+            "lambda": lam, "info": info}

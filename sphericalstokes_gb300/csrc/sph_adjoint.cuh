@@ -251,6 +251,82 @@ __global__ void k_bc_adjoint(KP<double> p, Adj a, BcStage st) {
     }
 }
 
+// The strain-rate law's part of the transposed Jacobian (k_edot_law, unrelaxed target
+// η_t = 2/(1/η_ini + 1/η_PL), η_PL = η_ini (ε̇_II/ε̇_bg)^m, m = (1-n)/n, ε̇_II of the clamped
+// interior cell s from sDD(s) and the 4-edge averages a, b, c of the shear rates):
+//   dη_t/dε̇ = m η_t² / (2 η_PL ε̇),  dε̇/dsDD = 1/(2ε̇),  dε̇/da = a/(4ε̇),  da/ds12(edge) = 1/4,
+//   sDD = ½ Σ D_ii²,  dη_t/dη_ini = η_t/η_ini,  dη_t/dn = -η_t² ln(ε̇/ε̇_bg) / (2 η_PL n²).
+// With g = λᵀ ∂R/∂η per cell (k_vjp_strain), NEWTON adds (∂η/∂V)ᵀ g to the velocity adjoint;
+// gEI and gN receive g dη_t/dη_ini and g dη_t/dn.  Phase cells (linear) have η = η_ini.
+template <int G, bool NEWTON>
+__global__ void __launch_bounds__(256) k_vjp_law(KP<double> p, Adj a, double* __restrict__ gEI, double* __restrict__ gN) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const double g = a.gEta[c];
+    const double ei = p.eta_ini[c];
+    if (p.phase && p.phase[c]) {
+        gEI[c] = g;
+        gN[c] = 0.0;
+        return;
+    }
+    const int si = clampi(i, 1, d.n1 - 2), sj = clampi(j, 1, d.n2 - 2), sk = clampi(k, 1, d.n3 - 2);
+    const int s = si + sy * sj + sz * sk;
+    const double q4 = 0.25;
+    const int e = s - 1 - sy - sz;
+    const double av = (p.s12[e] + p.s12[e + sy] + p.s12[e + 1] + p.s12[e + 1 + sy]) * q4;
+    const double bv = (p.s13[e] + p.s13[e + sz] + p.s13[e + 1] + p.s13[e + 1 + sz]) * q4;
+    const double cv = (p.s23[e] + p.s23[e + sz] + p.s23[e + sy] + p.s23[e + sy + sz]) * q4;
+    const double ed = sqrt(p.sDD[s] + q4 * (av * av + bv * bv + cv * cv));
+    const double n = p.n_exp, m = (1.0 - n) / n;
+    const double pl = ei * pow(ed / p.edot_bg, m);
+    const double et = 2.0 / (1.0 / ei + 1.0 / pl);
+    gEI[c] = g * et / ei;
+    gN[c] = ed > 0.0 ? -g * et * et * log(ed / p.edot_bg) / (2.0 * pl * n * n) : 0.0;
+    if (!NEWTON || g == 0.0 || !(ed > 0.0)) return;
+    const double w = g * m * et * et / (2.0 * pl * ed);  // g dη_t/dε̇
+    // ε̇ -> sDD(s) -> D_ii(s) -> V around s
+    {
+        const double ws = w / (2.0 * ed);
+        const CellD<double> D = cell_strain<double, G>(p.geo, p.d1, p.d2, p.d3, si, sj, p.V1[s], p.V1[s + 1], p.V2[s], p.V2[s + sy],
+                                                       p.V3[s], p.V3[s + sz]);
+        double* dst[6] = {a.aV1 + s, a.aV1 + s + 1, a.aV2 + s, a.aV2 + s + sy, a.aV3 + s, a.aV3 + s + sz};
+        for (int q = 0; q < 6; ++q) {
+            const CellD<double> u = cell_strain<double, G>(p.geo, p.d1, p.d2, p.d3, si, sj, q == 0 ? 1.0 : 0.0, q == 1 ? 1.0 : 0.0,
+                                                           q == 2 ? 1.0 : 0.0, q == 3 ? 1.0 : 0.0, q == 4 ? 1.0 : 0.0, q == 5 ? 1.0 : 0.0);
+            aadd(dst[q], ws * (D.D11 * u.D11 + D.D22 * u.D22 + D.D33 * u.D33));
+        }
+    }
+    // ε̇ -> the 4-edge averages -> each edge's shear rate -> its 4 velocities
+    const double wa = w * av / (4.0 * ed) * q4, wb = w * bv / (4.0 * ed) * q4, wc = w * cv / (4.0 * ed) * q4;
+    const int e12[4] = {e, e + sy, e + 1, e + 1 + sy};
+    for (int t = 0; t < 4; ++t) {
+        const int ec = e12[t];
+        const int ii = ec % sy, q = ec + sz;
+        double* dst[4] = {a.aV2 + q + sy, a.aV2 + q + sy + 1, a.aV1 + q + 1, a.aV1 + q + 1 + sy};
+        for (int u = 0; u < 4; ++u)
+            aadd(dst[u], wa * edge12<double, G>(p.geo, p.d1, p.d2, ii, u == 0 ? 1.0 : 0.0, u == 1 ? 1.0 : 0.0, u == 2 ? 1.0 : 0.0, u == 3 ? 1.0 : 0.0));
+    }
+    const int e13[4] = {e, e + sz, e + 1, e + 1 + sz};
+    for (int t = 0; t < 4; ++t) {
+        const int ec = e13[t];
+        const int ii = ec % sy, jj = (ec / sy) % d.py, q = ec + sy;
+        double* dst[4] = {a.aV3 + q + sz, a.aV3 + q + sz + 1, a.aV1 + q + 1, a.aV1 + q + 1 + sz};
+        for (int u = 0; u < 4; ++u)
+            aadd(dst[u], wb * edge13<double, G>(p.geo, p.d1, p.d3, ii, jj, u == 0 ? 1.0 : 0.0, u == 1 ? 1.0 : 0.0, u == 2 ? 1.0 : 0.0, u == 3 ? 1.0 : 0.0));
+    }
+    const int e23[4] = {e, e + sz, e + sy, e + sy + sz};
+    for (int t = 0; t < 4; ++t) {
+        const int ec = e23[t];
+        const int ii = ec % sy, jj = (ec / sy) % d.py, q = ec + 1;
+        double* dst[4] = {a.aV3 + q + sz, a.aV3 + q + sz + sy, a.aV2 + q + sy, a.aV2 + q + sy + sz};
+        for (int u = 0; u < 4; ++u)
+            aadd(dst[u], wc * edge23<double, G>(p.geo, p.d2, p.d3, ii, jj, u == 0 ? 1.0 : 0.0, u == 1 ? 1.0 : 0.0, u == 2 ? 1.0 : 0.0, u == 3 ? 1.0 : 0.0));
+    }
+}
+
 // pseudo-steps of the current viscosity (k_stress's DT_R) for the adjoint iteration
 __global__ void __launch_bounds__(256) k_pt_dtr(KP<double> p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;

@@ -1381,7 +1381,8 @@ static int write_file(const std::string& path, const void* data, size_t bytes) {
 // adjoint of the FP64 residual (sph_adjoint.cuh)
 enum AdjSlot {
     AJ_LV1, AJ_LV2, AJ_LV3, AJ_LP, AJ_S11, AJ_S22, AJ_S33, AJ_T12, AJ_T13, AJ_T23,
-    AJ_V1, AJ_V2, AJ_V3, AJ_P, AJ_GETA, AJ_GRHO, AJ_B1, AJ_B2, AJ_B3, AJ_BP, AJ_R1, AJ_R2, AJ_R3, AJ_RP, AJ_ETA, AJ_COUNT
+    AJ_V1, AJ_V2, AJ_V3, AJ_P, AJ_GETA, AJ_GRHO, AJ_B1, AJ_B2, AJ_B3, AJ_BP, AJ_R1, AJ_R2, AJ_R3, AJ_RP, AJ_ETA,
+    AJ_GEI, AJ_GN, AJ_COUNT
 };
 
 static int adj_alloc(Ctx* c) {
@@ -1465,6 +1466,10 @@ static int adj_apply(Ctx* c, KP<double>& p, bool with_bc) {
     k_vjp_momentum<G><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p, a);
     k_vjp_pressure<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);
     k_vjp_strain<G><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);
+    if (c->prm.rheology == SPH_RHEO_EDOT_POWER_RELAX)  // the law's dependence on V (Newton form) and its η_ini, n chain
+        k_vjp_law<G, true><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_GEI), adj_slot(c, AJ_GN));
+    else
+        CK(cudaMemcpyAsync(adj_slot(c, AJ_GEI), adj_slot(c, AJ_GETA), sizeof(double) * c->d.vol, cudaMemcpyDeviceToDevice, c->stream));
     if (with_bc) {
         KP<double> hp = p;
         hp.sig2 = 0.0; hp.sig3 = 0.0;
@@ -1691,6 +1696,23 @@ int sph_residual_vjp(void* h, const double* lV1, const double* lV2, const double
         (rc = adj_download(c, AJ_GETA, SPH_FIELD_P, g_eta)) || (rc = adj_download(c, AJ_GRHO, SPH_FIELD_P, g_rho)))
         return rc;
     CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_residual_vjp_law(void* h, double* g_eta_ini, double* g_n) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (!c->adj) return fail(SPH_ERR_INVALID, "sph_residual_vjp_law: no sph_residual_vjp before");
+    int rc = adj_download(c, AJ_GEI, SPH_FIELD_P, g_eta_ini);
+    if (rc) return rc;
+    if (g_n) {
+        *g_n = 0.0;
+        if (c->prm.rheology == SPH_RHEO_EDOT_POWER_RELAX) {
+            std::vector<double> h((size_t)c->prm.n1 * c->prm.n2 * c->prm.n3);
+            if ((rc = adj_download(c, AJ_GN, SPH_FIELD_P, h.data()))) return rc;
+            for (double v : h) *g_n += v;
+        }
+    }
     return SPH_OK;
 }
 

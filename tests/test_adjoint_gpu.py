@@ -101,3 +101,67 @@ def test_gradients_match_central_differences(bc):
         fd = (J_at(rho=rho0 + eps * d) - J_at(rho=rho0 - eps * d)) / (2 * eps)
         ad = float(np.sum(grad["drho"] * d))
         assert abs(fd - ad) <= 1e-5 * abs(fd), (fd, ad)
+
+
+def _law_params(n=(13, 11, 9)):
+    return S.sector_params(n, bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                           sig_bc=(0.0, 0.5, -0.5), incl_linear=1, vr=10.0)
+
+
+def test_vjp_of_the_power_law_residual_is_its_transposed_jacobian():
+    """nonlinear residual (η from the strain-rate law): ⟨λ, J v⟩ with J v by central differences"""
+    rng = np.random.default_rng(3)
+    with S.Solver(_law_params()) as sv:
+        sv.step(300)  # a state with non-trivial strain rates
+        u = {f: sv.get(f) for f in FIELDS}
+        v = _rand(sv, rng)
+        lam = _rand(sv, rng)
+        scale = max(np.abs(u[f]).max() for f in FIELDS)
+        eps = 1e-6 * scale
+
+        def R(w):
+            for f in FIELDS:
+                sv.set(f, w[f])
+            return A.residual_fields(sv)
+        rp = R({f: u[f] + eps * v[f] for f in FIELDS})
+        rm = R({f: u[f] - eps * v[f] for f in FIELDS})
+        Jv = {f: (rp[f] - rm[f]) / (2 * eps) for f in FIELDS}
+        R(u)
+        g = A.vjp(sv, lam, interior=False)
+    lhs, rhs = _dot(lam, Jv), _dot(g, v)
+    scale = sum(float(np.sum(np.abs(lam[f] * Jv[f]))) for f in FIELDS)
+    assert abs(lhs - rhs) <= 1e-6 * scale, (lhs, rhs, scale)
+
+
+def test_power_law_gradients_match_central_differences():
+    p = _law_params()
+    rng = np.random.default_rng(5)
+    with S.Solver(p) as sv:
+        _converged(sv)
+        base = {f: sv.get(f) for f in ("V1", "V2", "V3", "P", "TAU11", "TAU22", "TAU33", "TAU12", "TAU13", "TAU23", "ETA")}
+        grad = A.gradient(sv, tol=1e-12)
+        assert grad["info"].status == S.SPH_OK, (grad["info"].status, grad["info"].err)
+        ei0, rho0 = sv.get("ETA_INI"), sv.get("RHO")
+
+        def J_at(ei=None, rho=None, n=None):
+            for f, a in base.items():
+                sv.set(f, a)
+            sv.set("ETA_INI", ei0 if ei is None else ei)
+            sv.set("RHO", rho0 if rho is None else rho)
+            S.set_params(p, n_exp=3.0 if n is None else n)
+            sv.update_params(p)
+            _converged(sv)
+            return A.surface_misfit(sv)[0]
+
+        eps = 1e-4
+        for _ in range(2):
+            d = np.asfortranarray(rng.standard_normal(ei0.shape))
+            fd = (J_at(ei=ei0 * np.exp(eps * d)) - J_at(ei=ei0 * np.exp(-eps * d))) / (2 * eps)
+            ad = float(np.sum(grad["dlogeta_ini"] * d))
+            assert abs(fd - ad) <= 1e-5 * abs(fd), ("eta_ini", fd, ad)
+        fd = (J_at(n=3.0 + eps) - J_at(n=3.0 - eps)) / (2 * eps)
+        assert abs(fd - grad["dn"]) <= 1e-5 * abs(fd), ("n", fd, grad["dn"])
+        d = np.asfortranarray(rng.standard_normal(rho0.shape))
+        fd = (J_at(rho=rho0 + eps * d) - J_at(rho=rho0 - eps * d)) / (2 * eps)
+        ad = float(np.sum(grad["drho"] * d))
+        assert abs(fd - ad) <= 1e-5 * abs(fd), ("rho", fd, ad)

@@ -267,8 +267,9 @@ int sph_residual_vjp(void* ctx, const double* lV1, const double* lV2, const doub
 int sph_residual_vjp_law(void* ctx, double* g_eta_ini, double* g_n);
 
 /* Transposed PT solve (no counterpart in the reference): λ with Aᵀ λ = b, A the residual's
- * Jacobian in the interior-unknown form of sph_residual_vjp, iterated on the device with the
- * forward scheme's pseudo-steps (DT_R for the velocity rows, KBDT for the pressure rows).
+ * Jacobian in the interior-unknown form of sph_residual_vjp, iterated on the device by the
+ * forward scheme transposed: its pseudo-steps (DT_R for the velocity rows, KBDT for the
+ * pressure rows) and its stress relaxation, applied to a transposed stress memory.
  * b and λ in the layouts of sph_residual_vjp; λ holds the initial guess on entry.  Stops when
  * max|Aᵀλ - b| <= opts->tol * max|b| (checked every opts->nout iterations) or after
  * opts->maxiter.  Returns the solve status (SPH_OK, SPH_ERR_NOT_CONVERGED, SPH_ERR_DIVERGED). */

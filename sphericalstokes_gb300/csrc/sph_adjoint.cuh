@@ -338,38 +338,83 @@ __global__ void __launch_bounds__(256) k_pt_dtr(KP<double> p) {
     p.DT_R[c] = p.vpdt2 / (kb + gs * (e / (e + gs)));
 }
 
-// adjoint PT update (transposed system): λ_V += avg(DT_R) (Aᵀλ - b)_V at interior nodes,
-// λ_P -= KBDT (Aᵀλ - b)_P at cells — the forward pseudo-steps on the transposed rows
-__global__ void __launch_bounds__(256) k_adjoint_update(KP<double> p, Adj a, double* lV1, double* lV2, double* lV3, double* lP,
-                                                        const double* bV1, const double* bV2, const double* bV3, const double* bP,
-                                                        double* rV1, double* rV2, double* rV3, double* rP) {
+// Transposed PT with the forward scheme's stress memory.  The forward PT relaxes
+// τ toward 2η E(V) at the rate 1 - f (f = η/(η + GSDT); edges: avg4 η, avg4 GSDT) and
+// drives V with the momentum of τ.  The transposed iteration relaxes the memory μ toward
+// 2η M_τᵀ λ_V (M_τᵀ λ_V = aτ from k_vjp_momentum + k_vjp_pressure) at the same rate and
+// drives λ_V with Eᵀ μ: the coupling products are the transposes of the forward ones.
+// Here μ is updated and handed to k_vjp_strain as aτ = μ / (2η) (edges μ / avg4 η),
+// so that kernel forms Eᵀ μ.
+__global__ void __launch_bounds__(256) k_adj_memory(KP<double> p, Adj a, double* __restrict__ m11, double* __restrict__ m22,
+                                                    double* __restrict__ m33, double* __restrict__ m12, double* __restrict__ m13,
+                                                    double* __restrict__ m23) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const double q4 = 0.25;
+    {
+        const double e = p.eta[c], gs = p.gsc * p.etaSM[c];
+        const double w = gs / (e + gs);  // 1 - f
+        const double e2 = 2.0 * e;
+        double* m[3] = {m11, m22, m33};
+        double* t[3] = {a.aS11, a.aS22, a.aS33};
+        for (int q = 0; q < 3; ++q) {
+            const double mu = m[q][c] + w * (e2 * t[q][c] - m[q][c]);
+            m[q][c] = mu;
+            t[q][c] = mu / e2;
+        }
+    }
+    auto edge = [&](double* mu, double* at, int q, int o1, int o2, int o3) {
+        const double aE = (p.eta[q] + p.eta[q + o1] + p.eta[q + o2] + p.eta[q + o3]) * q4;
+        const double aG = p.gsc * ((p.etaSM[q] + p.etaSM[q + o1] + p.etaSM[q + o2] + p.etaSM[q + o3]) * q4);
+        const double w = aG / (aE + aG);
+        const double v = mu[c] + w * (aE * at[c] - mu[c]);
+        mu[c] = v;
+        at[c] = v / aE;
+    };
+    if (i < d.n1 - 1 && j < d.n2 - 1 && k < d.n3 - 2) edge(m12, a.aT12, c + sz, sy, 1, 1 + sy);
+    if (i < d.n1 - 1 && j < d.n2 - 2 && k < d.n3 - 1) edge(m13, a.aT13, c + sy, sz, 1, 1 + sz);
+    if (i < d.n1 - 2 && j < d.n2 - 1 && k < d.n3 - 1) edge(m23, a.aT23, c + 1, sz, sy, sy + sz);
+}
+
+// λ_P of the transposed PT: λ_P -= KBDT (M_Pᵀ λ_V - b_P), before the velocity rows use it
+__global__ void __launch_bounds__(256) k_adj_pressure_update(KP<double> p, Adj a, double* __restrict__ lP, const double* __restrict__ bP) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
+    const Dims& d = p.d;
+    if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
+    const int c = i + d.sy * j + d.sz * k;
+    lP[c] -= p.kbc * p.etaSM[c] * (a.aP[c] - bP[c]);
+}
+
+// λ_V of the transposed PT: λ_V += avg(DT_R) (Eᵀ μ + Dᵀ λ_P - b_V) at interior nodes
+__global__ void __launch_bounds__(256) k_adj_velocity_update(KP<double> p, Adj a, double* lV1, double* lV2, double* lV3,
+                                                             const double* bV1, const double* bV2, const double* bV3) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y * blockDim.y + threadIdx.y + 1, k = blockIdx.z + 1;
+    const Dims& d = p.d;
+    if (i > d.n1 - 1 || j > d.n2 - 1 || k > d.n3 - 1) return;
+    const int sy = d.sy, sz = d.sz;
+    const int c = i + sy * j + sz * k;
+    const double h = 0.5;
+    if (j <= d.n2 - 2 && k <= d.n3 - 2) lV1[c] += (a.aV1[c] - bV1[c]) * ((p.DT_R[c - 1] + p.DT_R[c]) * h);
+    if (i <= d.n1 - 2 && k <= d.n3 - 2) lV2[c] += (a.aV2[c] - bV2[c]) * ((p.DT_R[c - sy] + p.DT_R[c]) * h);
+    if (i <= d.n1 - 2 && j <= d.n2 - 2) lV3[c] += (a.aV3[c] - bV3[c]) * ((p.DT_R[c - sz] + p.DT_R[c]) * h);
+}
+
+// residual of the transposed system, r = Aᵀλ - b (convergence check)
+__global__ void __launch_bounds__(256) k_adj_residual(KP<double> p, Adj a, const double* bV1, const double* bV2, const double* bV3,
+                                                      const double* bP, double* rV1, double* rV2, double* rV3, double* rP) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y, k = blockIdx.z;
     const Dims& d = p.d;
     if (i > d.n1 || j > d.n2 || k > d.n3) return;
     const int sy = d.sy, sz = d.sz;
     const int c = i + sy * j + sz * k;
-    const double h = 0.5;
     const bool in1 = i >= 1 && i <= d.n1 - 1, in2 = j >= 1 && j <= d.n2 - 1, in3 = k >= 1 && k <= d.n3 - 1;
-    if (in1 && in2 && in3 && j <= d.n2 - 2 && k <= d.n3 - 2) {
-        const double r = a.aV1[c] - bV1[c];
-        rV1[c] = r;
-        lV1[c] += r * ((p.DT_R[c - 1] + p.DT_R[c]) * h);
-    }
-    if (in1 && in2 && in3 && i <= d.n1 - 2 && k <= d.n3 - 2) {
-        const double r = a.aV2[c] - bV2[c];
-        rV2[c] = r;
-        lV2[c] += r * ((p.DT_R[c - sy] + p.DT_R[c]) * h);
-    }
-    if (in1 && in2 && in3 && i <= d.n1 - 2 && j <= d.n2 - 2) {
-        const double r = a.aV3[c] - bV3[c];
-        rV3[c] = r;
-        lV3[c] += r * ((p.DT_R[c - sz] + p.DT_R[c]) * h);
-    }
-    if (i < d.n1 && j < d.n2 && k < d.n3) {
-        const double r = a.aP[c] - bP[c];
-        rP[c] = r;
-        lP[c] -= p.kbc * p.etaSM[c] * r;
-    }
+    rV1[c] = (in1 && in2 && in3 && j <= d.n2 - 2 && k <= d.n3 - 2) ? a.aV1[c] - bV1[c] : 0.0;
+    rV2[c] = (in1 && in2 && in3 && i <= d.n1 - 2 && k <= d.n3 - 2) ? a.aV2[c] - bV2[c] : 0.0;
+    rV3[c] = (in1 && in2 && in3 && i <= d.n1 - 2 && j <= d.n2 - 2) ? a.aV3[c] - bV3[c] : 0.0;
+    rP[c] = (i < d.n1 && j < d.n2 && k < d.n3) ? a.aP[c] - bP[c] : 0.0;
 }
 
 }  // namespace sph

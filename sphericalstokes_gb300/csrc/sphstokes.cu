@@ -1382,7 +1382,7 @@ static int write_file(const std::string& path, const void* data, size_t bytes) {
 enum AdjSlot {
     AJ_LV1, AJ_LV2, AJ_LV3, AJ_LP, AJ_S11, AJ_S22, AJ_S33, AJ_T12, AJ_T13, AJ_T23,
     AJ_V1, AJ_V2, AJ_V3, AJ_P, AJ_GETA, AJ_GRHO, AJ_B1, AJ_B2, AJ_B3, AJ_BP, AJ_R1, AJ_R2, AJ_R3, AJ_RP, AJ_ETA,
-    AJ_GEI, AJ_GN, AJ_COUNT
+    AJ_GEI, AJ_GN, AJ_M11, AJ_M22, AJ_M33, AJ_M12, AJ_M13, AJ_M23, AJ_COUNT
 };
 
 static int adj_alloc(Ctx* c) {
@@ -1498,18 +1498,40 @@ static int adjoint_solve_g(Ctx* c, const sph_solve_opts& o, sph_solve_info* inf)
     double bmax = 0.0;
     for (int s = 0; s < 4; ++s) bmax = std::max(bmax, slot_val(*c, s));
     if (bmax == 0.0) bmax = 1.0;
+    for (int s = AJ_M11; s <= AJ_M23; ++s) CK(cudaMemsetAsync(adj_slot(c, s), 0, sizeof(double) * c->d.vol, c->stream));
+    const bool law = c->prm.rheology == SPH_RHEO_EDOT_POWER_RELAX;
     dim3 gu((c->d.n1 + 1 + 31) / 32, (c->d.n2 + 1 + 7) / 8, c->d.n3 + 1);
     int64_t it = 0;
     double err = 1.0;
     int status = SPH_ERR_NOT_CONVERGED;
     while (it < o.maxiter) {
         ++it;
-        if ((rc = adj_apply<G>(c, p, true))) return rc;
-        k_adjoint_update<<<gu, blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_LV1), adj_slot(c, AJ_LV2), adj_slot(c, AJ_LV3),
-                                                        adj_slot(c, AJ_LP), adj_slot(c, AJ_B1), adj_slot(c, AJ_B2), adj_slot(c, AJ_B3),
-                                                        adj_slot(c, AJ_BP), adj_slot(c, AJ_R1), adj_slot(c, AJ_R2), adj_slot(c, AJ_R3),
-                                                        adj_slot(c, AJ_RP));
+        // M_τᵀ λ_V (σ adjoints -> τ adjoints) and M_Pᵀ λ_V
+        CK(cudaMemsetAsync(adj_slot(c, AJ_S11), 0, sizeof(double) * c->d.vol * (AJ_GRHO - AJ_S11 + 1), c->stream));
+        k_vjp_momentum<G><<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p, a);
+        k_vjp_pressure<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);
+        k_adj_pressure_update<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_LP), adj_slot(c, AJ_BP));
+        k_adj_memory<<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_M11), adj_slot(c, AJ_M22), adj_slot(c, AJ_M33),
+                                                                  adj_slot(c, AJ_M12), adj_slot(c, AJ_M13), adj_slot(c, AJ_M23));
+        k_vjp_strain<G><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a);  // Eᵀ μ + Dᵀ λ_P
+        if (law) k_vjp_law<G, true><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_GEI), adj_slot(c, AJ_GN));
+        {
+            KP<double> hp = p;
+            hp.sig2 = 0.0; hp.sig3 = 0.0;
+            for (auto st = c->bc.rbegin(); st != c->bc.rend(); ++st) {
+                int eu = st->dim == 0 ? c->d.n2 + 1 : c->d.n1 + 1;
+                int ev = st->dim == 2 ? c->d.n2 + 1 : c->d.n3 + 1;
+                dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
+                k_bc_adjoint<G><<<g, blk2d(), 0, c->stream>>>(hp, a, *st);
+            }
+        }
+        k_adj_velocity_update<<<grid_vel(c->d), blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_LV1), adj_slot(c, AJ_LV2), adj_slot(c, AJ_LV3),
+                                                                         adj_slot(c, AJ_B1), adj_slot(c, AJ_B2), adj_slot(c, AJ_B3));
         if (it % nout) continue;
+        // convergence: the transposed residual Aᵀλ - b of the current λ
+        if ((rc = adj_apply<G>(c, p, true))) return rc;
+        k_adj_residual<<<gu, blk2d(), 0, c->stream>>>(p, a, adj_slot(c, AJ_B1), adj_slot(c, AJ_B2), adj_slot(c, AJ_B3), adj_slot(c, AJ_BP),
+                                                      adj_slot(c, AJ_R1), adj_slot(c, AJ_R2), adj_slot(c, AJ_R3), adj_slot(c, AJ_RP));
         CK(cudaMemsetAsync(c->red, 0, sizeof(unsigned long long) * kRedSlots, c->stream));
         for (int s = 0; s < 4; ++s) launch_maxabs<double>(*c, adj_slot(c, AJ_R1 + s), nullptr, s);
         if ((rc = fetch_red(*c))) return rc;

@@ -266,6 +266,24 @@ int sph_residual_vjp(void* ctx, const double* lV1, const double* lV2, const doub
  * V (the Jacobian of the residual as the forward solver defines it). */
 int sph_residual_vjp_law(void* ctx, double* g_eta_ini, double* g_n);
 
+/* Explicit advection of nf <= 4 cell fields (pressure-array size, reference layout) by the
+ * current velocities over dt: first-order upwinding written as a central difference plus a
+ * |v|-scaled diffusion, with |v| smoothed to sqrt(v² + delta²) so that the step is
+ * differentiable where a velocity component changes sign (delta = 0: plain upwinding);
+ * cell-mean velocities and the geometry's metric factors (diapir ascent between solves; the
+ * scripts run one time step, so there is no counterpart in the reference). */
+int sph_advect(void* ctx, double dt, double delta, int32_t nf, const double* const* phi, double* const* phi_new);
+
+/* Transpose of sph_advect at the same velocities, phi, dt and delta: mu = (∂phi_new/∂phi)ᵀ mu_new
+ * per field, aV1..aV3 = (∂phi_new/∂V)ᵀ mu_new summed over the fields (velocity-array sizes,
+ * every entry). */
+int sph_advect_vjp(void* ctx, double dt, double delta, int32_t nf, const double* const* phi, const double* const* mu_new,
+                   double* const* mu, double* aV1, double* aV2, double* aV3);
+
+/* In place: the transposed homogeneous BC program on velocity adjoints (adjoint with respect to
+ * every entry -> with respect to the interior entries; boundary entries come out zero). */
+int sph_bc_vjp(void* ctx, double* aV1, double* aV2, double* aV3);
+
 /* Transposed PT solve (no counterpart in the reference): λ with Aᵀ λ = b, A the residual's
  * Jacobian in the interior-unknown form of sph_residual_vjp, iterated on the device by the
  * forward scheme transposed: its pseudo-steps (DT_R for the velocity rows, KBDT for the

@@ -114,6 +114,11 @@ _SIGS = {
     "sph_residual_fields": ([C.c_void_p] + [C.POINTER(C.c_double)] * 4, C.c_int),
     "sph_residual_vjp": ([C.c_void_p] + [C.POINTER(C.c_double)] * 10 + [C.c_int32], C.c_int),
     "sph_residual_vjp_law": ([C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)], C.c_int),
+    "sph_advect": ([C.c_void_p, C.c_double, C.c_double, C.c_int32, C.POINTER(C.POINTER(C.c_double)),
+                    C.POINTER(C.POINTER(C.c_double))], C.c_int),
+    "sph_advect_vjp": ([C.c_void_p, C.c_double, C.c_double, C.c_int32] + [C.POINTER(C.POINTER(C.c_double))] * 3
+                       + [C.POINTER(C.c_double)] * 3, C.c_int),
+    "sph_bc_vjp": ([C.c_void_p] + [C.POINTER(C.c_double)] * 3, C.c_int),
     "sph_adjoint_solve": ([C.c_void_p] + [C.POINTER(C.c_double)] * 8 + [C.POINTER(SolveOpts), C.POINTER(SolveInfo)], C.c_int),
     "sph_save": ([C.c_void_p, C.c_char_p, C.c_int32, C.c_double, C.c_double, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                   C.c_int64], C.c_int),

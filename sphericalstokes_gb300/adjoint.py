@@ -68,7 +68,8 @@ def law_vjp(sv: Solver) -> tuple[np.ndarray, float]:
 def adjoint_solve(sv: Solver, b: dict, tol: float = 1e-10, maxiter: int = 1_000_000, nout: int = 500, lam0: dict | None = None):
     """λ with (∂R/∂u)ᵀ λ = b (interior-unknown form); returns (λ, SolveInfo)."""
     bs = [_fortran(b.get(f)) for f in VEL + ("P",)]
-    lam = {f: (_fortran(lam0[f]).copy() if lam0 and f in lam0 else _empty(sv, f)) for f in VEL + ("P",)}
+    lam = {f: (np.array(lam0[f], dtype=np.float64, order="F", copy=True) if lam0 and f in lam0 else _empty(sv, f))
+           for f in VEL + ("P",)}
     info = SolveInfo()
     o = make_opts(tol=tol, maxiter=maxiter, nout=nout)
     rc = sv.lib.sph_adjoint_solve(sv._h, *[_ptr(a) for a in bs], *[_ptr(lam[f]) for f in VEL + ("P",)], C.byref(o), C.byref(info))

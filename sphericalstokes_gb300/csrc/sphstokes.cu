@@ -31,6 +31,7 @@
 #include "sph_fused.cuh"
 #include "sph_sweep_x2.cuh"
 #include "sph_adjoint.cuh"
+#include "sph_advect.cuh"
 #include "sphstokes.h"
 
 using namespace sph;
@@ -1718,6 +1719,90 @@ int sph_residual_vjp(void* h, const double* lV1, const double* lV2, const double
         (rc = adj_download(c, AJ_GETA, SPH_FIELD_P, g_eta)) || (rc = adj_download(c, AJ_GRHO, SPH_FIELD_P, g_rho)))
         return rc;
     CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_advect(void* h, double dt, double delta, int32_t nf, const double* const* phi, double* const* phi_new) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || (nf > 0 && (!phi || !phi_new))) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (nf < 1 || nf > 4) return fail(SPH_ERR_INVALID, "sph_advect: 1 to 4 fields");
+    int rc = sync64(*c);
+    if (rc || (rc = adj_alloc(c))) return rc;
+    AdvFields F;
+    F.nf = nf;
+    for (int f = 0; f < nf; ++f) {
+        if ((rc = adj_upload(c, AJ_B1 + f, SPH_FIELD_P, phi[f]))) return rc;
+        F.in[f] = adj_slot(c, AJ_B1 + f);
+        F.out[f] = adj_slot(c, AJ_R1 + f);
+    }
+    KP<double> p = make_kp<double>(*c, c->s64);
+    const int G = c->prm.geometry;
+    if (G == SPH) k_advect<SPH><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, dt, delta);
+    else if (G == CYL) k_advect<CYL><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, dt, delta);
+    else k_advect<CART><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, dt, delta);
+    CK(cudaGetLastError());
+    for (int f = 0; f < nf; ++f)
+        if ((rc = adj_download(c, AJ_R1 + f, SPH_FIELD_P, phi_new[f]))) return rc;
+    return SPH_OK;
+}
+
+int sph_advect_vjp(void* h, double dt, double delta, int32_t nf, const double* const* phi, const double* const* mu_new, double* const* mu,
+                   double* aV1, double* aV2, double* aV3) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !phi || !mu_new || !mu) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (nf < 1 || nf > 4) return fail(SPH_ERR_INVALID, "sph_advect_vjp: 1 to 4 fields");
+    int rc = sync64(*c);
+    if (rc || (rc = adj_alloc(c))) return rc;
+    AdvFields F, M;
+    F.nf = M.nf = nf;
+    for (int f = 0; f < nf; ++f) {
+        if ((rc = adj_upload(c, AJ_B1 + f, SPH_FIELD_P, phi[f])) || (rc = adj_upload(c, AJ_R1 + f, SPH_FIELD_P, mu_new[f])) ||
+            (rc = adj_upload(c, AJ_M11 + f, SPH_FIELD_P, nullptr)))
+            return rc;
+        F.in[f] = adj_slot(c, AJ_B1 + f);
+        M.in[f] = adj_slot(c, AJ_R1 + f);
+        M.out[f] = adj_slot(c, AJ_M11 + f);
+    }
+    for (int s = AJ_V1; s <= AJ_V3; ++s) CK(cudaMemsetAsync(adj_slot(c, s), 0, sizeof(double) * c->d.vol, c->stream));
+    KP<double> p = make_kp<double>(*c, c->s64);
+    double *a1 = adj_slot(c, AJ_V1), *a2 = adj_slot(c, AJ_V2), *a3 = adj_slot(c, AJ_V3);
+    const int G = c->prm.geometry;
+    if (G == SPH) k_advect_vjp<SPH><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, M, a1, a2, a3, dt, delta);
+    else if (G == CYL) k_advect_vjp<CYL><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, M, a1, a2, a3, dt, delta);
+    else k_advect_vjp<CART><<<grid_cells(c->d), blk2d(), 0, c->stream>>>(p, F, M, a1, a2, a3, dt, delta);
+    CK(cudaGetLastError());
+    for (int f = 0; f < nf; ++f)
+        if ((rc = adj_download(c, AJ_M11 + f, SPH_FIELD_P, mu[f]))) return rc;
+    if ((rc = adj_download(c, AJ_V1, SPH_FIELD_V1, aV1)) || (rc = adj_download(c, AJ_V2, SPH_FIELD_V2, aV2)) ||
+        (rc = adj_download(c, AJ_V3, SPH_FIELD_V3, aV3)))
+        return rc;
+    return SPH_OK;
+}
+
+int sph_bc_vjp(void* h, double* aV1, double* aV2, double* aV3) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !aV1 || !aV2 || !aV3) return fail(SPH_ERR_INVALID, "NULL argument");
+    int rc = sync64(*c);
+    if (rc || (rc = adj_alloc(c))) return rc;
+    if ((rc = adj_upload(c, AJ_V1, SPH_FIELD_V1, aV1)) || (rc = adj_upload(c, AJ_V2, SPH_FIELD_V2, aV2)) ||
+        (rc = adj_upload(c, AJ_V3, SPH_FIELD_V3, aV3)))
+        return rc;
+    KP<double> p = make_kp<double>(*c, c->s64);
+    p.sig2 = 0.0; p.sig3 = 0.0;
+    Adj a = adj_ptrs(c);
+    const int G = c->prm.geometry;
+    for (auto st = c->bc.rbegin(); st != c->bc.rend(); ++st) {
+        int eu = st->dim == 0 ? c->d.n2 + 1 : c->d.n1 + 1;
+        int ev = st->dim == 2 ? c->d.n2 + 1 : c->d.n3 + 1;
+        dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
+        if (G == SPH) k_bc_adjoint<SPH><<<g, blk2d(), 0, c->stream>>>(p, a, *st);
+        else if (G == CYL) k_bc_adjoint<CYL><<<g, blk2d(), 0, c->stream>>>(p, a, *st);
+        else k_bc_adjoint<CART><<<g, blk2d(), 0, c->stream>>>(p, a, *st);
+    }
+    CK(cudaGetLastError());
+    if ((rc = adj_download(c, AJ_V1, SPH_FIELD_V1, aV1)) || (rc = adj_download(c, AJ_V2, SPH_FIELD_V2, aV2)) ||
+        (rc = adj_download(c, AJ_V3, SPH_FIELD_V3, aV3)))
+        return rc;
     return SPH_OK;
 }
 

@@ -329,6 +329,21 @@ def run_ours(args) -> None:
         if solve_info["mixed"]["converged"] and solve_info["fp64"]["converged"]:
             solve_info["speedup_mixed_vs_fp64"] = round(solve_info["fp64"]["seconds"] / solve_info["mixed"]["seconds"], 2)
 
+    plateau_info = None
+    if args.plateau_sweeps > 0:
+        from sphericalstokes_gb300 import plateau as PL
+
+        ep = PL.EllipsePlateau()
+        with PL.ellipse_solver(ep, "mixed") as sv:
+            sv.sweep(args.warmup)
+            ms = sv.sweep(args.plateau_sweeps)
+        cells = ep.nr * ep.nth * ep.nph
+        plateau_info = {"grid": [ep.nr, ep.nth, ep.nph], "sweeps": args.plateau_sweeps,
+                        "ms_per_sweep": round(ms / args.plateau_sweeps, 4),
+                        "teff_gbs": round(26 * cells * 4 / (ms / args.plateau_sweeps * 1e-3) / 1e9, 1),
+                        "setup": "elliptical plateau on a 40°x40° shell, 200 km deep + 20 km sticky air, n=3 crust over "
+                                 "linear mantle (ratio 1e-2), seeded ±2% density field; FP32 correction sweeps"}
+
     batch_info = None
     if args.batch > 0:
         from sphericalstokes_gb300 import batch as B
@@ -371,6 +386,8 @@ def run_ours(args) -> None:
         line["time_to_tol"] = solve_info
     if batch_info:
         line["batch"] = batch_info
+    if plateau_info:
+        line["plateau_511x255x255"] = plateau_info
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(n, seconds=args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -402,6 +419,8 @@ def main():
     ap.add_argument("--batch-edges", default="31,47", help="grid edges the batched solves draw from")
     ap.add_argument("--batch-budget", type=int, default=20000, help="sweep budget per batched solve")
     ap.add_argument("--batch-threads", type=int, default=16)
+    ap.add_argument("--plateau-sweeps", type=int, default=200,
+                    help="sweeps timed on the 511x255x255 elliptical-plateau grid (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

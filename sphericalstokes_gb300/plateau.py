@@ -203,3 +203,106 @@ def run(setup: PlateauSetup, precision: str = "fp64", steps: int = 8, maxiter: i
     finally:
         if own:
             sv.close()
+
+
+# ---------------------------------------------------------------------------
+# Elliptical plateau on a curved shell (a larger plateau experiment built on the same
+# solver): crust of 35 km outside and 70 km inside an elliptical plateau (semi-axes
+# 12° x 6°) with a cos² taper over 2°, a seeded Gaussian random density perturbation,
+# a power-law crust over a linear mantle; the topography load enters through a sticky-air
+# layer above the reference surface, as in the reference plateau experiment.
+@dataclass
+class EllipsePlateau:
+    nr: int = 511
+    nth: int = 255
+    nph: int = 255
+    R_km: float = 6371.0
+    depth_km: float = 200.0
+    air_km: float = 20.0            # sticky-air layer above the reference surface
+    extent_deg: float = 40.0        # θ and φ extent
+    semi_deg: tuple = (12.0, 6.0)   # ellipse semi-axes along θ and φ
+    taper_deg: float = 2.0
+    crust_km: tuple = (35.0, 70.0)  # outside / inside the plateau
+    rho_crust: float = 2800.0
+    rho_mantle: float = 3300.0
+    rho_air: float = 0.0
+    drho_frac: float = 0.02         # amplitude of the random density perturbation
+    corr_km: float = 20.0           # correlation length of the random field
+    seed: int = 0
+    n_exp: float = 3.0
+    eta_ratio: float = 1e-2         # crust / mantle viscosity
+    eta_air: float = 1e-3           # air / mantle viscosity
+    dmp: float = 4.5
+
+    def params(self, precision: str = "mixed", **kw) -> Params:
+        """Spherical shell r in [R - depth, R + air], scaled by the depth; stress-free
+        mantle-scale units (η_mantle = 1, ρ_mantle = 1, g = 1)."""
+        from . import default_params
+
+        L = self.depth_km
+        r0, r1 = (self.R_km - self.depth_km) / L, (self.R_km + self.air_km) / L
+        ext = math.radians(self.extent_deg)
+        p = default_params("spherical")
+        vr = 1.0 / min(self.eta_ratio, self.eta_air)
+        set_params(p, precision=precision, bc="free_slip", rheology="edot_power_relax", n_exp=self.n_exp, relax=0.5,
+                   edot_bg=1.0, init="none", n1=self.nr, n2=self.nth, n3=self.nph, c1=0.5 * (r0 + r1), l1=r1 - r0,
+                   c2=math.pi / 2, l2=ext, c3=0.0, l3=ext, l_ref=r1 - r0, r=self.R_km / L, dmp=self.dmp, g=1.0,
+                   vr=vr, vpdt=0.0, eta0=1.0, rho0=1.0, sh=0.0, incl_linear=1)
+        set_params(p, **kw)
+        return p
+
+    def crust_thickness_km(self, th: np.ndarray, ph: np.ndarray) -> np.ndarray:
+        """35 km outside, 70 km inside the ellipse, cos² taper over ``taper_deg`` outside its edge
+        (distance measured along the ray from the centre in the ellipse's own scaling)."""
+        a, b = (math.radians(x) for x in self.semi_deg)
+        dth, dph = th - math.pi / 2, ph
+        e = np.sqrt((dth / a) ** 2 + (dph / b) ** 2)          # 1 on the ellipse
+        rad = np.sqrt(dth ** 2 + dph ** 2)
+        edge = np.where(e > 0, rad / np.maximum(e, 1e-300), a)  # ellipse radius along this ray
+        dist = np.degrees(np.maximum(e - 1.0, 0.0) * edge)      # angular distance beyond the edge
+        w = np.where(e <= 1.0, 1.0, np.where(dist < self.taper_deg, np.cos(0.5 * math.pi * dist / self.taper_deg) ** 2, 0.0))
+        return self.crust_km[0] + (self.crust_km[1] - self.crust_km[0]) * w
+
+    def random_field(self, shape: tuple, spacing_km: tuple) -> np.ndarray:
+        """Seeded Gaussian random field (PCG64 white noise smoothed by a Gaussian kernel of
+        ``corr_km``), scaled to max |f| = 1."""
+        rng = np.random.default_rng(self.seed)
+        f = rng.standard_normal(shape)
+        F = np.fft.rfftn(f)
+        k = [np.fft.fftfreq(n, d=h) for n, h in zip(shape[:-1], spacing_km[:-1])] + [np.fft.rfftfreq(shape[-1], d=spacing_km[-1])]
+        K2 = sum(np.meshgrid(*[kk ** 2 for kk in k], indexing="ij"))
+        F *= np.exp(-0.5 * (2 * math.pi) ** 2 * K2 * self.corr_km ** 2)
+        g = np.fft.irfftn(F, s=shape, axes=tuple(range(len(shape))))
+        return g / np.abs(g).max()
+
+    def fields(self, p: Params) -> dict:
+        """ρ, η_ini and the phase flag (1: linear mantle / air) in the reference layout."""
+        L = self.depth_km
+        x1, x2, x3 = linspace(p.c1, p.l1, p.n1), linspace(p.c2, p.l2, p.n2), linspace(p.c3, p.l3, p.n3)
+        R, T, F = np.meshgrid(x1, x2, x3, indexing="ij")
+        depth = (self.R_km / L - R) * L                       # km below the reference surface
+        hc = self.crust_thickness_km(T, F)
+        air, crust = depth < 0.0, (depth >= 0.0) & (depth < hc)
+        rm = 1.0
+        rho = np.full(R.shape, rm)
+        rho[crust] = self.rho_crust / self.rho_mantle
+        rho[air] = self.rho_air / self.rho_mantle
+        mid = self.R_km - 0.5 * self.depth_km
+        sp = (p.l1 * L / (p.n1 - 1), p.l2 * mid / (p.n2 - 1), p.l3 * mid / (p.n3 - 1))
+        noise = self.random_field(R.shape, sp)
+        rho = np.where(air, rho, rho * (1.0 + self.drho_frac * noise))
+        eta = np.ones(R.shape)
+        eta[crust] = self.eta_ratio
+        eta[air] = self.eta_air
+        phase = np.where(crust, 0.0, 1.0)
+        return {"RHO": np.asfortranarray(rho), "ETA_INI": np.asfortranarray(eta), "ETA": np.asfortranarray(eta),
+                "PHASE": np.asfortranarray(phase)}
+
+
+def ellipse_solver(setup: EllipsePlateau, precision: str = "mixed", **kw) -> Solver:
+    """A solver holding the elliptical-plateau fields."""
+    p = setup.params(precision, **kw)
+    sv = Solver(p)
+    for f, a in setup.fields(p).items():
+        sv.set(f, a)
+    return sv

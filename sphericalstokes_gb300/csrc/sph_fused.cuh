@@ -316,6 +316,17 @@ __device__ __forceinline__ void tma_load3d(float* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// edge stress update from the sums of the 4 surrounding cells' ηSM and η with
+// gsc4 = GSDT/ηSM / 4: (τ + aG D) aE / (aE + aG), aG = gsc4 s4, aE = e4 / 4
+__device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4, float e4, float D) {
+    const float aG = gsc4 * s4;
+    return (told + aG * D) * pdiv(e4, fmaf(4.f, aG, e4));
+}
+
+// Waiting: warp 0 alone waits on the mbarriers of the planes a step needs and
+// the block barrier that follows passes the completed copies on to the other
+// warps, so nine of ten warps never poll.
+//
 // Thread roles (10 warps): warp w < 8 owns the row J = y0 + w of the tile, lane
 // l the column I = x0 + l: it computes the stage-1 point (I, J) (a = l+1,
 // b = w+1) and then the velocity node (I, J), taking its own point's stresses,
@@ -398,7 +409,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     // this thread's stage-1 point of the current plane, and carried values of the previous plane
     float o11 = 0.f, o22 = 0.f, o33 = 0.f, odt = 0.f, ov1 = 0.f, ov2 = 0.f, ov3 = 0.f;
     float p33 = 0.f, pdt = 0.f, p13 = 0.f, p23 = 0.f;
-
+    const float gsc4 = 0.25f * gsc;
     auto stage1 = [&](int k, bool own_plane) {
         if (!s1_thread) return;
         const float* I0 = S.in[(k + 3) % 3][0] + iin;
@@ -429,19 +440,19 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             }
             if (e12_xy && k < n3 - 2) {
                 const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
-                v12 = edge_update(old(I12), gsc, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
+                v12 = edge_update_q(old(I12), gsc4, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
                                   in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
                 if (own) o.t12[g] = v12;
             }
             if (e13_xy && k < n3 - 1) {
                 const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
-                v13 = edge_update(old(I13), gsc, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
+                v13 = edge_update_q(old(I13), gsc4, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
                                   in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
                 if (own) o.t13[g] = v13;
             }
             if (e23_xy && k < n3 - 1) {
                 const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
-                v23 = edge_update(old(I23), gsc, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
+                v23 = edge_update_q(old(I23), gsc4, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
                                   in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
                 if (own) o.t23[g] = v23;
             }
@@ -492,30 +503,38 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         issue_inputs(kA + 1);
         issue_old(kA);
     }
-    wait_in(kA - 1);
-    wait_in(kA);
-    wait_old(kA - 1);
+    const bool waiter = warp == 0;
+    if (waiter) {
+        wait_in(kA - 1);
+        wait_in(kA);
+        wait_old(kA - 1);
+    }
+    __syncthreads();
     if (kA >= 1) {
         stage1(kA - 1, false);
         p33 = o33;
         pdt = odt;
     }
     for (int K = kA; K < kB; ++K) {
-        __syncthreads();  // every thread is done with the slots of plane K-1
+        if (waiter) {
+            wait_in(K + 1);
+            wait_old(K);
+        }
+        __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
         if (tid == 0) {
             issue_inputs(K + 2);
             issue_old(K + 1);
         }
-        wait_in(K + 1);
-        wait_old(K);
         stage1(K, true);
         __syncthreads();
         velocity(K);
     }
     // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
-    wait_in(kB + 1);
-    wait_old(kB);
-    if (!ok && err) atomicExch(err, 1);
+    if (waiter) {
+        wait_in(kB + 1);
+        wait_old(kB);
+        if (!ok && err) atomicExch(err, 1);
+    }
 }
 
 inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }

@@ -108,7 +108,8 @@ struct Ctx {
     bool use_tma = true;
     bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
     bool fused = true;   // FP32 sweeps use the fused kernel
-    int fused_chunk = 0; // planes per block of the fused sweep
+    int fused_chunk = 0; // planes per block of the fused sweep (0: chosen by fused_chunk())
+    int fused_slots = 0; // resident blocks of the fused TMA sweep on the device (SMs x blocks per SM)
     double* adj = nullptr;  // adjoint arrays (AJ_COUNT slots of the box), allocated on first use
     // per-launch timing of the fused sweep kernel (sph_sweep_profile): event pairs
     // recorded around each launch while prof_next < prof_ev.size()/2
@@ -457,13 +458,26 @@ void swap_state(State<float>& s) {
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int, int>, int> g_tuned_chunk;
 
+// x3 chunk length of the fused sweep.  Each block marches over one chunk of
+// planes and pays about two planes more than it owns (the halo plane below the
+// chunk and the pipeline fill), while the hardware scheduler balances the SMs
+// only to within one block at the end of the launch.  The time model
+// (k + 2.5) * (blocks / slots + 0.7), slots = resident blocks on the device, picks
+// the chunk among 4..24 planes; at 63^3, 127^3 and 255^3 its pick is within
+// 1 % of the fastest chunk measured on a GB300 (sph_autotune measures instead).
 int fused_chunk(const Ctx& c) {
     if (c.fused_chunk > 0) return c.fused_chunk;
-    const long long xy = (long long)((c.d.n1 + FTX - 1) / FTX) * ((c.d.n2 + FTY - 1) / FTY);
-    long long nch = (152LL * 3 + xy - 1) / xy;  // about three resident blocks per SM (one wave)
-    if (nch < 1) nch = 1;
-    int k = (int)((c.d.n3 + nch - 1) / nch);
-    return k < 4 ? 4 : k;
+    const double xy = (double)((c.d.n1 + FTX - 1) / FTX) * ((c.d.n2 + FTY - 1) / FTY);
+    const double slots = c.fused_slots > 0 ? c.fused_slots : 456.0;
+    int best = 4;
+    double best_t = 1e300;
+    for (int k : {4, 6, 8, 12, 16, 24}) {
+        const double blocks = xy * ((c.d.n3 + k - 1) / k);
+        const double t = (k + 2.5) * (blocks / slots + 0.7);
+        if (t < best_t) { best_t = t; best = k; }
+        if (k >= c.d.n3) break;
+    }
+    return best;
 }
 
 template <int G, int MODE>
@@ -1153,6 +1167,13 @@ int sph_create(const sph_params* prm, void** out) {
         c->has32 = true;
     }
     if ((rc = set_fused_attrs())) return cleanup(rc);
+    {
+        int dev = 0, sms = 0, per_sm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tma<SPH, 1>, FNT, fused_tma_smem_bytes()) == cudaSuccess)
+            c->fused_slots = sms * per_sm;
+        cudaGetLastError();
+    }
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;

@@ -68,6 +68,16 @@ struct KP {
     unsigned long long* red;           // reduction slots (max of |x| as ordered bits)
 };
 
+// Programmatic dependent launch: wait until the preceding grid of the stream has
+// completed and its writes are visible (returns at once for a launch without a
+// programmatic dependency), then allow the next grid of the stream to be
+// scheduled, so its launch overlaps this grid instead of following it.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_enter() {
+    pdl_wait();
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
 __host__ __device__ inline int clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 // pressure of a boundary cell under the far-field normal-stress BC: the total

@@ -336,6 +336,7 @@ __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4,
 template <int G, int MODE>
 __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
                                                        int* __restrict__ err) {
+    pdl_wait();  // no early release of the next grid: its blocks would take SM slots in this grid's tail
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TmaSmem& S = *reinterpret_cast<TmaSmem*>(smem_raw);
     enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-tile slots (IX: rP | ρ)

@@ -365,6 +365,7 @@ __device__ __forceinline__ T* vfield(const KP<T>& p, int f) { return f == 0 ? p.
 
 template <typename T, int G>
 __global__ void k_bc(KP<T> p, BcStage st, int homog) {
+    pdl_enter();
     const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
     const Dims& d = p.d;
     const int D = st.dim;

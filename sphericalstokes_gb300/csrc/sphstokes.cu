@@ -107,6 +107,7 @@ struct Ctx {
     int* d_err = nullptr;                // set by a kernel whose bounded wait ran out
     bool use_tma = true;
     bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
+    bool use_pdl = true;  // sweep and BC kernels launched with a programmatic dependency (pdl_enter)
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep (0: chosen by fused_chunk())
     int fused_slots = 0; // resident blocks of the fused TMA sweep on the device (SMs x blocks per SM)
@@ -185,6 +186,23 @@ KP<T> make_kp(Ctx& c, State<T>& s) {
 }
 
 dim3 blk2d() { return dim3(32, 8, 1); }
+
+// launch with a programmatic dependency on the preceding grid of the stream (the
+// kernel starts with pdl_enter()); a plain launch when PDL is switched off
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(bool pdl, void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args) {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<KArgs>(args)...);
+}
 dim3 grid_cells(const Dims& d) { return dim3((d.n1 + 31) / 32, (d.n2 + 7) / 8, d.n3); }
 dim3 grid_vel(const Dims& d) { return dim3((d.n1 - 1 + 31) / 32, (d.n2 - 1 + 7) / 8, d.n3 - 1); }
 
@@ -250,7 +268,7 @@ void launch_bc(Ctx& c, KP<T>& p, int homog) {
         int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1;
         int ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
         dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
-        k_bc<T, G><<<g, blk2d(), 0, c.stream>>>(p, st, homog);
+        launch_pdl(c.use_pdl, k_bc<T, G>, g, blk2d(), 0, c.stream, p, st, homog);
     }
 }
 
@@ -860,7 +878,7 @@ void correction_sweep(Ctx& c) {
             if (c.use_x2)
                 k_sweep_x2<G><<<grid, dim3(X2_NT, 1, 1), sweep_x2_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
             else
-                k_fused_tma<G, 1><<<grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
+                launch_pdl(c.use_pdl, k_fused_tma<G, 1>, grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream, q, o, kc, maps, c.d_err);
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
         } else {
             const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
@@ -1177,6 +1195,7 @@ int sph_create(const sph_params* prm, void** out) {
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
+    if (const char* e = std::getenv("SPH_NO_PDL")) c->use_pdl = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
     if ((rc = init_fields(*c))) return cleanup(rc);
     if ((rc = compute_f_scale(*c))) return cleanup(rc);

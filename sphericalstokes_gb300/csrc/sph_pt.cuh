@@ -356,7 +356,10 @@ __global__ void __launch_bounds__(256) k_tau_visc(KP<T> p) {
 // x_cd is the cell-centre coordinate of the node along axis cd.  In the
 // homogeneous form (correction problem) constants vanish: LIN -> 0,
 // LIN2M -> -A[in], sig -> 0.
-enum BcKind { BC_NEG = 0, BC_COPY = 1, BC_ZERO = 2, BC_LIN = 3, BC_LIN2M = 4, BC_STRESS = 5 };
+// BC_STRESS_SRC: BC_STRESS in a stage that also copies the two tangential fields
+// into their ghost layer; it reads those fields at the copies' source cells
+// instead of at the ghosts the copies are writing (the same values)
+enum BcKind { BC_NEG = 0, BC_COPY = 1, BC_ZERO = 2, BC_LIN = 3, BC_LIN2M = 4, BC_STRESS = 5, BC_STRESS_SRC = 6 };
 struct BcOp { int field; int kind; int cd; double c0, c1; };
 struct BcStage { int dim; int nops; BcOp op[3]; };
 
@@ -405,7 +408,8 @@ __global__ void k_bc(KP<T> p, BcStage st, int homog) {
                 }
                 default: {  // BC_STRESS: normal ghost of V2 (D == 1) or V3 (D == 2) from div V = 0 in the boundary cell
                     const int cellb = side == 0 ? 0 : ext[D] - 2;        // boundary cell index along D
-                    const int cc = base + cellb * stride[D];             // boundary cell
+                    // boundary cell (its tangential velocities: at the ghost, or at the source of its copy)
+                    const int cc = base + (op.kind == BC_STRESS_SRC ? cellb + (side == 0 ? 1 : -1) : cellb) * stride[D];
                     const int i = (D == 0) ? cellb : u;
                     const int j = (D == 1) ? cellb : (du == 1 ? u : v);
                     const CellMetric<T> m = cell_metric<T, G>(p, i, j);

@@ -87,7 +87,8 @@ struct Ctx {
     uint8_t* phase = nullptr;
     unsigned long long* red = nullptr;   // device reduction slots
     unsigned long long* hred = nullptr;  // pinned host copy
-    std::vector<BcStage> bc;
+    std::vector<BcStage> bc;      // BC program: ghost-velocity stages in the reference order (the adjoint transposes these)
+    std::vector<BcStage> bc_run;  // the program launched by launch_bc: bc, or an equivalent one with fewer stages
     double cur_n = 1.0;
     double f_scale = 1.0;
     double last_ms = 0.0;
@@ -221,9 +222,19 @@ BcStage stage(int dim, std::initializer_list<BcOp> ops) {
     return s;
 }
 
+int build_bc_program(Ctx& c);
 int build_bc(Ctx& c) {
+    const int rc = build_bc_program(c);
+    if (rc == SPH_OK && c.bc_run.empty()) c.bc_run = c.bc;
+    return rc;
+}
+
+// the ghost-velocity stages of the BC set (Julia reference order), in c.bc; a
+// shorter equivalent program for the launches goes to c.bc_run where one exists
+int build_bc_program(Ctx& c) {
     const sph_params& q = c.prm;
     c.bc.clear();
+    c.bc_run.clear();
     const double rsh = q.r * q.sh;
     if (q.bc == SPH_BC_FREE_SLIP) {  // SphericalStokes_plateau.jl:64-92
         c.bc.push_back(stage(0, {op(0, BC_NEG), op(1, BC_COPY), op(2, BC_COPY)}));
@@ -238,6 +249,12 @@ int build_bc(Ctx& c) {
         c.bc.push_back(stage(1, {op(1, BC_STRESS)}));
         c.bc.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY)}));
         c.bc.push_back(stage(2, {op(2, BC_STRESS)}));
+        // the launched program: each copy stage merged with the stress stage after it,
+        // whose op then reads the copies' sources (same values, three launches)
+        c.bc_run.clear();
+        c.bc_run.push_back(c.bc[0]);
+        c.bc_run.push_back(stage(1, {op(0, BC_COPY), op(2, BC_COPY), op(1, BC_STRESS_SRC)}));
+        c.bc_run.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY), op(2, BC_STRESS_SRC)}));
         return SPH_OK;
     }
     if (q.bc != SPH_BC_DIAPIR) return fail(SPH_ERR_INVALID, "unknown bc");
@@ -264,7 +281,7 @@ int build_bc(Ctx& c) {
 
 template <typename T, int G>
 void launch_bc(Ctx& c, KP<T>& p, int homog) {
-    for (const BcStage& st : c.bc) {
+    for (const BcStage& st : c.bc_run) {
         int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1;
         int ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
         dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
@@ -1311,7 +1328,6 @@ int sph_update_params(void* h, const sph_params* p) {
     }
     c->graph_len = 0;
     c->corr_ready = false;
-    c->bc.clear();
     if ((rc = build_bc(*c))) return rc;
     return compute_f_scale(*c);
 }

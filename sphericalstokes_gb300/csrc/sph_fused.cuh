@@ -316,6 +316,12 @@ __device__ __forceinline__ void tma_load3d(float* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// store at a 32-bit unsigned byte offset from a field's base: the address is the
+// base plus a zero-extended register, with no 64-bit index arithmetic per store
+__device__ __forceinline__ void st_at(float* base, unsigned byte_off, float v) {
+    *reinterpret_cast<float*>(reinterpret_cast<char*>(base) + byte_off) = v;
+}
+
 // edge stress update from the sums of the 4 surrounding cells' ηSM and η with
 // gsc4 = GSDT/ηSM / 4: (τ + aG D) aE / (aE + aG), aG = gsc4 s4, aE = e4 / 4
 __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4, float e4, float D) {
@@ -421,6 +427,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         auto old = [&](int f) { return O[f * TOLD_TILE]; };
         const bool own = own_plane && s1_own;
         const int g = gxy + d.sz * k;
+        const unsigned gb = 4u * (unsigned)g;  // byte offset (owned points only: g >= 0)
         float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
         if (s1_in) {
             {
@@ -437,25 +444,25 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
                 v33 = (old(I33) + 2.f * gs * D.D33) * f;
                 if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
                 vdt = pdiv(vpdt2, kb + gs * f);
-                if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
+                if (own) { st_at(o.P, gb, vP); st_at(o.t11, gb, v11); st_at(o.t22, gb, v22); st_at(o.t33, gb, v33); }
             }
             if (e12_xy && k < n3 - 2) {
                 const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
                 v12 = edge_update_q(old(I12), gsc4, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
                                   in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
-                if (own) o.t12[g] = v12;
+                if (own) st_at(o.t12, gb, v12);
             }
             if (e13_xy && k < n3 - 1) {
                 const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
                 v13 = edge_update_q(old(I13), gsc4, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
                                   in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
-                if (own) o.t13[g] = v13;
+                if (own) st_at(o.t13, gb, v13);
             }
             if (e23_xy && k < n3 - 1) {
                 const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
                 v23 = edge_update_q(old(I23), gsc4, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
                                   in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
-                if (own) o.t23[g] = v23;
+                if (own) st_at(o.t23, gb, v23);
             }
         }
         o11 = v11 - vP; o22 = v22 - vP; o33 = v33 - vP; odt = vdt;
@@ -473,24 +480,25 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         const float c13 = C0[E13][ty][tx], c23 = C0[E23][ty][tx];
         if (K >= 1 && K <= n3 - 1) {
             const int g = gIJ + d.sz * K;
+            const unsigned gb = 4u * (unsigned)g;
             const float h = 0.5f;
             const float t12a = C1[E12][ty + 1][tx], t12b = C1[E12][ty][tx];
             if (m1_xy && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
                 float r = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
                                            t12a, t12b, c13, p13);
                 if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
-                o.V1[g] = ov1 + r * ((C0[QDT][ty + 1][tx] + odt) * h);
+                st_at(o.V1, gb, ov1 + r * ((C0[QDT][ty + 1][tx] + odt) * h));
             }
             if (m2_xy && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
                 float r = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
                                            c23, p23);
                 if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
-                o.V2[g] = ov2 + r * ((C0[QDT][ty][tx + 1] + odt) * h);
+                st_at(o.V2, gb, ov2 + r * ((C0[QDT][ty][tx + 1] + odt) * h));
             }
             if (m3_xy) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
                 float r = mom3_m<float, G>(mm, d1, d2, d3, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
                 if (MODE == 1) r += S.rv[K & 1][2][ty * FTX + tx];
-                o.V3[g] = ov3 + r * ((pdt + odt) * h);
+                st_at(o.V3, gb, ov3 + r * ((pdt + odt) * h));
             }
         }
         p13 = c13; p23 = c23; p33 = o33; pdt = odt;

@@ -1082,6 +1082,9 @@ int check_params(const sph_params* p) {
     if (!(p->l1 > 0 && p->l2 > 0 && p->l3 > 0 && p->l_ref > 0)) return fail(SPH_ERR_INVALID, "lengths must be positive");
     long long px = ((p->n1 + 1 + 31) / 32) * 32LL;
     if (px * (p->n2 + 1LL) * (p->n3 + 1LL) >= (1LL << 31)) return fail(SPH_ERR_INVALID, "grid too large for 32-bit indexing");
+    // the fused FP32 sweep stores at 32-bit byte offsets (4 bytes x box index < 2^32)
+    if (p->precision != SPH_PREC_FP64 && px * (p->n2 + 1LL) * (p->n3 + 1LL) >= (1LL << 30))
+        return fail(SPH_ERR_INVALID, "grid too large for the FP32 sweep (box of 2^30 points or more)");
     if (p->geometry == SPH_GEOM_SPHERICAL) {
         if (p->c1 - p->l1 / 2 <= 0) return fail(SPH_ERR_INVALID, "spherical radius range must be positive");
         if (p->c2 - p->l2 / 2 <= 0 || p->c2 + p->l2 / 2 >= kPi) return fail(SPH_ERR_INVALID, "colatitude range must be inside (0, pi)");

@@ -76,6 +76,10 @@ def test_invalid_params_rejected_without_device_work():
     assert lib.sph_create(C.byref(p), C.byref(h)) == S.SPH_ERR_INVALID
     p = S.default_params("spherical", c2=0.1, l2=1.0)
     assert lib.sph_create(C.byref(p), C.byref(h)) == S.SPH_ERR_INVALID
+    # 1024 x 1023 x 1023 cells: a box of 2^30 points, past the FP32 sweep's 32-bit byte offsets
+    p = S.default_params("spherical", n1=1023, n2=1023, n3=1023, precision="mixed")
+    assert lib.sph_create(C.byref(p), C.byref(h)) == S.SPH_ERR_INVALID
+    assert b"FP32 sweep" in lib.sph_last_error()
     assert lib.sph_step(None, 1) == S.SPH_ERR_INVALID
     assert lib.sph_destroy(None) == 0
 

@@ -22,6 +22,8 @@
 // MODE 0: reference iteration (ρg body force).  MODE 1: correction problem of
 // the mixed-precision solve (right-hand sides rP, rV; η and ηSM frozen).
 #pragma once
+#include <type_traits>
+
 #include "sph_core.cuh"
 
 namespace sph {
@@ -404,6 +406,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
     const EdgeMetric<float> em = edge_metric<float, G>(p.geo, x, y, n1, n2);
     const int gxy = x + d.sy * y;
+    const bool y_face = y == 0 || y == n2 - 1;  // stage-1 point on an x2 face of the box
     const int iin = b * TIN_X + a + 3;   // input-tile index of the stage-1 point
     const int iold = b * TOLD_X + a + 3; // old-tile index of the stage-1 point
     const int tx = lane, ty = warp;      // velocity node (warps < FTY)
@@ -417,10 +420,13 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     float o11 = 0.f, o22 = 0.f, o33 = 0.f, odt = 0.f, ov1 = 0.f, ov2 = 0.f, ov3 = 0.f;
     float p33 = 0.f, pdt = 0.f, p13 = 0.f, p23 = 0.f;
     const float gsc4 = 0.25f * gsc;
-    auto stage1 = [&](int k, bool own_plane) {
+    // stage1 / velocity of an interior plane (1 <= k <= n3 - 3: every x3 condition holds
+    // and no x3 face is a traction face) when `inner` is std::true_type
+    auto stage1 = [&](int k, bool own_plane, int sk, auto inner) {
+        constexpr bool IN = decltype(inner)::value;
         if (!s1_thread) return;
-        const float* I0 = S.in[(k + 3) % 3][0] + iin;
-        const float* I1 = S.in[(k + 4) % 3][0] + iin;
+        const float* I0 = S.in[sk][0] + iin;
+        const float* I1 = S.in[sk == 2 ? 0 : sk + 1][0] + iin;
         auto in0 = [&](int f, int db, int da) { return I0[f * TIN_TILE + db * TIN_X + da]; };
         auto in1 = [&](int f, int db, int da) { return I1[f * TIN_TILE + db * TIN_X + da]; };
         const float* O = &S.old[k & 1][0][0] + iold;
@@ -428,43 +434,53 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         const bool own = own_plane && s1_own;
         const int g = gxy + d.sz * k;
         const unsigned gb = 4u * (unsigned)g;  // byte offset (owned points only: g >= 0)
-        float vP = 0.f, v11 = 0.f, v22 = 0.f, v33 = 0.f, vdt = 0.f, v12 = 0.f, v13 = 0.f, v23 = 0.f;
-        if (s1_in) {
-            {
-                ov1 = in0(0, 0, 0); ov2 = in0(1, 0, 0); ov3 = in0(2, 0, 0);
-                const CellD<float> D = cell_strain_m<float, G>(cm, d1, ov1, in0(0, 0, 1), ov2, in0(1, 1, 0), ov3, in1(2, 0, 0));
-                const float sm = in0(4, 0, 0), e = in0(3, 0, 0);
-                const float gs = gsc * sm, kb = kbc * sm;
-                const float f = pdiv(e, e + gs);
-                float dv = D.div;
-                if (MODE == 1) dv += old(IX);
-                vP = old(IP) - kb * dv;
-                v11 = (old(I11) + 2.f * gs * D.D11) * f;
-                v22 = (old(I22) + 2.f * gs * D.D22) * f;
-                v33 = (old(I33) + 2.f * gs * D.D33) * f;
-                if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
-                vdt = pdiv(vpdt2, kb + gs * f);
-                if (own) { st_at(o.P, gb, vP); st_at(o.t11, gb, v11); st_at(o.t22, gb, v22); st_at(o.t33, gb, v33); }
+        // every stage-1 thread evaluates all stencils (the tiles hold finite or zero-filled
+        // values at points outside the box); validity masks only the stores and the ring
+        const bool k12 = IN || k < n3 - 2, k1x = IN || k < n3 - 1;
+        ov1 = in0(0, 0, 0); ov2 = in0(1, 0, 0); ov3 = in0(2, 0, 0);
+        float vP, v11, v22, v33, vdt, v12, v13, v23;
+        {
+            const CellD<float> D = cell_strain_m<float, G>(cm, d1, ov1, in0(0, 0, 1), ov2, in0(1, 1, 0), ov3, in1(2, 0, 0));
+            const float sm = in0(4, 0, 0), e = in0(3, 0, 0);
+            const float gs = gsc * sm, kb = kbc * sm;
+            const float f = pdiv(e, e + gs);
+            float dv = D.div;
+            if (MODE == 1) dv += old(IX);
+            vP = old(IP) - kb * dv;
+            v11 = (old(I11) + 2.f * gs * D.D11) * f;
+            v22 = (old(I22) + 2.f * gs * D.D22) * f;
+            v33 = (old(I33) + 2.f * gs * D.D33) * f;
+            if (IN) {
+                if (p.traction && y_face) vP = v22 - p.sig2;
+            } else if (p.traction) {
+                traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
             }
-            if (e12_xy && k < n3 - 2) {
-                const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
-                v12 = edge_update_q(old(I12), gsc4, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
-                                  in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
-                if (own) st_at(o.t12, gb, v12);
-            }
-            if (e13_xy && k < n3 - 1) {
-                const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
-                v13 = edge_update_q(old(I13), gsc4, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
-                                  in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
-                if (own) st_at(o.t13, gb, v13);
-            }
-            if (e23_xy && k < n3 - 1) {
-                const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
-                v23 = edge_update_q(old(I23), gsc4, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
-                                  in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
-                if (own) st_at(o.t23, gb, v23);
-            }
+            vdt = pdiv(vpdt2, kb + gs * f);
         }
+        {
+            const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
+            v12 = edge_update_q(old(I12), gsc4, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
+                                in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
+        }
+        {
+            const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
+            v13 = edge_update_q(old(I13), gsc4, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
+                                in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
+        }
+        {
+            const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
+            v23 = edge_update_q(old(I23), gsc4, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
+                                in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
+        }
+        const bool ok12 = s1_in && e12_xy && k12, ok13 = s1_in && e13_xy && k1x, ok23 = s1_in && e23_xy && k1x;
+        if (own && s1_in) { st_at(o.P, gb, vP); st_at(o.t11, gb, v11); st_at(o.t22, gb, v22); st_at(o.t33, gb, v33); }
+        if (own && ok12) st_at(o.t12, gb, v12);
+        if (own && ok13) st_at(o.t13, gb, v13);
+        if (own && ok23) st_at(o.t23, gb, v23);
+        if (!s1_in) { vP = 0.f; v11 = 0.f; v22 = 0.f; v33 = 0.f; vdt = 0.f; }
+        if (!ok12) v12 = 0.f;
+        if (!ok13) v13 = 0.f;
+        if (!ok23) v23 = 0.f;
         o11 = v11 - vP; o22 = v22 - vP; o33 = v33 - vP; odt = vdt;
         float (*W)[FSY][FSX] = S.st[k & 1];
         W[Q11][b][a] = o11; W[Q22][b][a] = o22; W[Q33][b][a] = o33;
@@ -472,24 +488,25 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     };
 
     // velocities of plane K from the stresses of planes K-1 and K
-    auto velocity = [&](int K) {
+    auto velocity = [&](int K, auto inner) {
+        constexpr bool IN = decltype(inner)::value;
         if (!v_ok) return;
         float (*C0)[FSY][FSX] = S.st[K & 1];
         float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
-        if (K == kA) { p13 = C1[E13][ty][tx]; p23 = C1[E23][ty][tx]; }
+        if (!IN && K == kA) { p13 = C1[E13][ty][tx]; p23 = C1[E23][ty][tx]; }
         const float c13 = C0[E13][ty][tx], c23 = C0[E23][ty][tx];
-        if (K >= 1 && K <= n3 - 1) {
+        if (IN || (K >= 1 && K <= n3 - 1)) {
             const int g = gIJ + d.sz * K;
             const unsigned gb = 4u * (unsigned)g;
             const float h = 0.5f;
             const float t12a = C1[E12][ty + 1][tx], t12b = C1[E12][ty][tx];
-            if (m1_xy && K <= n3 - 2) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
+            if (m1_xy && (IN || K <= n3 - 2)) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
                 float r = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
                                            t12a, t12b, c13, p13);
                 if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
                 st_at(o.V1, gb, ov1 + r * ((C0[QDT][ty + 1][tx] + odt) * h));
             }
-            if (m2_xy && K <= n3 - 2) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
+            if (m2_xy && (IN || K <= n3 - 2)) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
                 float r = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
                                            c23, p23);
                 if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
@@ -519,12 +536,13 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         wait_old(kA - 1);
     }
     __syncthreads();
+    int sk = (kA + 2) % 3;  // input-ring slot of plane kA - 1
     if (kA >= 1) {
-        stage1(kA - 1, false);
+        stage1(kA - 1, false, sk, std::false_type{});
         p33 = o33;
         pdt = odt;
     }
-    for (int K = kA; K < kB; ++K) {
+    auto step = [&](int K, auto inner) {
         if (waiter) {
             wait_in(K + 1);
             wait_old(K);
@@ -534,9 +552,15 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             issue_inputs(K + 2);
             issue_old(K + 1);
         }
-        stage1(K, true);
+        sk = sk == 2 ? 0 : sk + 1;
+        stage1(K, true, sk, inner);
         __syncthreads();
-        velocity(K);
+        velocity(K, inner);
+    };
+    step(kA, std::false_type{});  // (sets the carried edge stresses of plane kA - 1)
+    for (int K = kA + 1; K < kB; ++K) {
+        if (K <= n3 - 3) step(K, std::true_type{});
+        else step(K, std::false_type{});
     }
     // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
     if (waiter) {

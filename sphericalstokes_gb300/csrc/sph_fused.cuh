@@ -490,33 +490,33 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     // velocities of plane K from the stresses of planes K-1 and K
     auto velocity = [&](int K, auto inner) {
         constexpr bool IN = decltype(inner)::value;
-        if (!v_ok) return;
+        if (warp >= FTY) return;
         float (*C0)[FSY][FSX] = S.st[K & 1];
         float (*C1)[FSY][FSX] = S.st[(K - 1) & 1];
         if (!IN && K == kA) { p13 = C1[E13][ty][tx]; p23 = C1[E23][ty][tx]; }
         const float c13 = C0[E13][ty][tx], c23 = C0[E23][ty][tx];
         if (IN || (K >= 1 && K <= n3 - 1)) {
-            const int g = gIJ + d.sz * K;
-            const unsigned gb = 4u * (unsigned)g;
+            // all three updates evaluated by every row thread; validity masks the stores
+            const unsigned gb = 4u * (unsigned)(gIJ + d.sz * K);  // byte offset (valid nodes only: >= 0)
             const float h = 0.5f;
             const float t12a = C1[E12][ty + 1][tx], t12b = C1[E12][ty][tx];
-            if (m1_xy && (IN || K <= n3 - 2)) {  // V1 (I-1/2, J, K), cell m = (I-1, J, K)
-                float r = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
-                                           t12a, t12b, c13, p13);
-                if (MODE == 1) r += S.rv[K & 1][0][ty * FTX + tx];
-                st_at(o.V1, gb, ov1 + r * ((C0[QDT][ty + 1][tx] + odt) * h));
+            // V1 (I-1/2, J, K), cell m = (I-1, J, K)
+            float r1 = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
+                                        t12a, t12b, c13, p13);
+            // V2 (I, J-1/2, K), cell m = (I, J-1, K)
+            float r2 = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
+                                        c23, p23);
+            // V3 (I, J, K-1/2), cell m = (I, J, K-1)
+            float r3 = mom3_m<float, G>(mm, d1, d2, d3, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
+            if (MODE == 1) {
+                r1 += S.rv[K & 1][0][ty * FTX + tx];
+                r2 += S.rv[K & 1][1][ty * FTX + tx];
+                r3 += S.rv[K & 1][2][ty * FTX + tx];
             }
-            if (m2_xy && (IN || K <= n3 - 2)) {  // V2 (I, J-1/2, K), cell m = (I, J-1, K)
-                float r = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
-                                           c23, p23);
-                if (MODE == 1) r += S.rv[K & 1][1][ty * FTX + tx];
-                st_at(o.V2, gb, ov2 + r * ((C0[QDT][ty][tx + 1] + odt) * h));
-            }
-            if (m3_xy) {  // V3 (I, J, K-1/2), cell m = (I, J, K-1)
-                float r = mom3_m<float, G>(mm, d1, d2, d3, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
-                if (MODE == 1) r += S.rv[K & 1][2][ty * FTX + tx];
-                st_at(o.V3, gb, ov3 + r * ((pdt + odt) * h));
-            }
+            const bool kin = IN || K <= n3 - 2;
+            if (v_ok && m1_xy && kin) st_at(o.V1, gb, ov1 + r1 * ((C0[QDT][ty + 1][tx] + odt) * h));
+            if (v_ok && m2_xy && kin) st_at(o.V2, gb, ov2 + r2 * ((C0[QDT][ty][tx + 1] + odt) * h));
+            if (v_ok && m3_xy) st_at(o.V3, gb, ov3 + r3 * ((pdt + odt) * h));
         }
         p13 = c13; p23 = c23; p33 = o33; pdt = odt;
     };

@@ -241,11 +241,17 @@ class Solver:
     def dims(self, name: str) -> tuple[int, int, int]:
         return field_dims(self.params, name)
 
-    def get(self, name: str) -> np.ndarray:
-        """Field in the reference's layout: Fortran-ordered float64 array, A[i,j,k] = Julia A[i+1,j+1,k+1]."""
+    def get(self, name: str, out: np.ndarray | None = None) -> np.ndarray:
+        """Field in the reference's layout: Fortran-ordered float64 array, A[i,j,k] = Julia A[i+1,j+1,k+1].
+
+        ``out``: a Fortran-ordered float64 array of the field's shape to copy into (e.g. a view
+        of pinned host memory, which the device writes at full link speed); a new array if None."""
         fid = FIELDS[ALIASES.get(name, name)]
         shp = self.dims(name)
-        out = np.zeros(shp, dtype=np.float64, order="F")
+        if out is None:
+            out = np.zeros(shp, dtype=np.float64, order="F")
+        elif out.shape != shp or out.dtype != np.float64 or not out.flags.f_contiguous or not out.flags.writeable:
+            raise ValueError(f"{name}: out must be a writeable Fortran-ordered float64 array of shape {shp}")
         _check(self.lib, self.lib.sph_get_field(self._h, fid, out.ctypes.data_as(C.POINTER(C.c_double)), out.size), f"get {name}")
         return out
 

@@ -73,3 +73,20 @@ def test_save_reads_back_like_the_matlab_reader(tmp_path, geom):
         assert np.isfinite(divv).all()
         for name, f in (("D_RTH", "TAU12"), ("D_RZ", "TAU13"), ("D_THZ", "TAU23")):
             assert _fread(tmp_path / f"A_{name}.bin", got[f].shape).shape == got[f].shape
+
+
+def test_get_into_caller_array():
+    """Solver.get(out=...) fills a caller's Fortran-ordered array with what get() returns,
+    and refuses arrays of the wrong shape, type or order"""
+    p = S.default_params("spherical", n1=15, n2=13, n3=11, n_exp=3.0)
+    with S.Solver(p) as sv:
+        sv.step(5)
+        for f in ("V1", "P", "TAU12"):
+            ref = sv.get(f)
+            out = np.full(ref.shape, np.nan, order="F")
+            assert sv.get(f, out=out) is out
+            assert np.array_equal(out, ref)
+        with pytest.raises(ValueError):
+            sv.get("P", out=np.zeros(sv.dims("P")))  # C order
+        with pytest.raises(ValueError):
+            sv.get("P", out=np.zeros(sv.dims("V1"), order="F"))

@@ -324,6 +324,86 @@ __device__ __forceinline__ void st_at(float* base, unsigned byte_off, float v) {
     *reinterpret_cast<float*>(reinterpret_cast<char*>(base) + byte_off) = v;
 }
 
+// Per-thread coefficients of the FP32 sweep's edge-strain and momentum stencils:
+// the metric factors of sph_core.cuh (EdgeMetric at the stage-1 point, MomMetric
+// at the velocity node) multiplied out with the spacings once per thread, so that
+// each update below is a short chain of FMAs.  The expressions are those of
+// edge12_m .. mom3_m regrouped (2 (x h) = x, 3 (x h) = 1.5 x): the same values up
+// to FP32 rounding.
+struct SweepCoef {
+    float e12_d2, e12_h;          // τ12: iRh d2, iRh / 2
+    float e13_d3, e13_h;          // τ13: iRh iSc1 d3, iRh / 2
+    float e23_d2, e23_d3, e23_h;  // τ23: iRc1 d2, iRc1 iSh d3, iRc1 ctH / 2
+    float m1_d2, m1_d3, m1_n, m1_t;  // V1: iR1 d2, iR1 iS1 d3, normal-stress and shear metric terms
+    float m2_d2, m2_d3, m2_s, m2_n;  // V2: iR2 d2, iR2 iS2 d3, shear and normal-stress metric terms
+    float m3_d3, m3_s, m3_n;         // V3: iR2 iS3 d3, shear metric terms
+};
+template <int G>
+__device__ __forceinline__ SweepCoef sweep_coef(const EdgeMetric<float>& e, const MomMetric<float>& m, float d2, float d3) {
+    SweepCoef c;
+    if (G == SPH) {
+        c.e12_d2 = e.iRh * d2; c.e12_h = 0.5f * e.iRh;
+        c.e13_d3 = e.iRh * e.iSc1 * d3; c.e13_h = 0.5f * e.iRh;
+        c.e23_d2 = e.iRc1 * d2; c.e23_d3 = e.iRc1 * e.iSh * d3; c.e23_h = 0.5f * e.iRc1 * e.ctH;
+        c.m1_d2 = m.iR1 * d2; c.m1_d3 = m.iR1 * m.iS1 * d3; c.m1_n = m.iR1; c.m1_t = 0.5f * m.iR1 * m.ct1;
+        c.m2_d2 = m.iR2 * d2; c.m2_d3 = m.iR2 * m.iS2 * d3; c.m2_s = 1.5f * m.iR2; c.m2_n = 0.5f * m.iR2 * m.ct2;
+        c.m3_d3 = m.iR2 * m.iS3 * d3; c.m3_s = 1.5f * m.iR2; c.m3_n = m.iR2 * m.ct3;
+    } else if (G == CYL) {
+        c.e12_d2 = e.iRh * d2; c.e12_h = 0.5f * e.iRh;
+        c.e13_d3 = d3; c.e13_h = 0.f;
+        c.e23_d2 = e.iRc1 * d2; c.e23_d3 = d3; c.e23_h = 0.f;
+        c.m1_d2 = m.iR1 * d2; c.m1_d3 = d3; c.m1_n = 0.5f * m.iR1; c.m1_t = 0.f;
+        c.m2_d2 = m.iR2 * d2; c.m2_d3 = d3; c.m2_s = m.iR2; c.m2_n = 0.f;
+        c.m3_d3 = d3; c.m3_s = 0.5f * m.iR2; c.m3_n = 0.f;
+    } else {
+        c.e12_d2 = d2; c.e12_h = 0.f; c.e13_d3 = d3; c.e13_h = 0.f; c.e23_d2 = d2; c.e23_d3 = d3; c.e23_h = 0.f;
+        c.m1_d2 = d2; c.m1_d3 = d3; c.m1_n = 0.f; c.m1_t = 0.f;
+        c.m2_d2 = d2; c.m2_d3 = d3; c.m2_s = 0.f; c.m2_n = 0.f;
+        c.m3_d3 = d3; c.m3_s = 0.f; c.m3_n = 0.f;
+    }
+    return c;
+}
+// engineering shear strain rates at the edges (arguments as edge12_m .. edge23_m)
+template <int G>
+__device__ __forceinline__ float sw_edge12(const SweepCoef& c, float d1, float v2a, float v2b, float v1a, float v1b) {
+    const float t = fmaf(c.e12_d2, v1b - v1a, (v2b - v2a) * d1);
+    return G != CART ? fmaf(-c.e12_h, v2a + v2b, t) : t;
+}
+template <int G>
+__device__ __forceinline__ float sw_edge13(const SweepCoef& c, float d1, float v3a, float v3b, float v1a, float v1b) {
+    const float t = fmaf(c.e13_d3, v1b - v1a, (v3b - v3a) * d1);
+    return G == SPH ? fmaf(-c.e13_h, v3a + v3b, t) : t;
+}
+template <int G>
+__device__ __forceinline__ float sw_edge23(const SweepCoef& c, float v3a, float v3b, float v2a, float v2b) {
+    const float t = fmaf(c.e23_d3, v2b - v2a, c.e23_d2 * (v3b - v3a));
+    return G == SPH ? fmaf(-c.e23_h, v3a + v3b, t) : t;
+}
+// momentum residuals (arguments as mom1_m .. mom3_m)
+template <int G>
+__device__ __forceinline__ float sw_mom1(const SweepCoef& c, float d1, float s11m, float s11, float s22m, float s22, float s33m, float s33,
+                                         float ta, float tb, float ua, float ub) {
+    float r = fmaf(c.m1_d3, ua - ub, fmaf(c.m1_d2, ta - tb, (s11 - s11m) * d1));
+    if (G == SPH) r = fmaf(c.m1_t, ta + tb, fmaf(c.m1_n, fmaf(-0.5f, (s22m + s22) + (s33m + s33), s11m + s11), r));
+    if (G == CYL) r = fmaf(c.m1_n, (s11m + s11) - (s22m + s22), r);
+    return r;
+}
+template <int G>
+__device__ __forceinline__ float sw_mom2(const SweepCoef& c, float d1, float s22m, float s22, float s33m, float s33, float ta, float tb,
+                                         float ua, float ub) {
+    float r = fmaf(c.m2_d3, ua - ub, fmaf(c.m2_d2, s22 - s22m, (ta - tb) * d1));
+    if (G != CART) r = fmaf(c.m2_s, ta + tb, r);
+    if (G == SPH) r = fmaf(c.m2_n, (s22m + s22) - (s33m + s33), r);
+    return r;
+}
+template <int G>
+__device__ __forceinline__ float sw_mom3(const SweepCoef& c, float d1, float s33m, float s33, float ta, float tb, float ua, float ub) {
+    float r = fmaf(c.m3_d3, s33 - s33m, fmaf(c.m2_d2, ua - ub, (ta - tb) * d1));
+    if (G != CART) r = fmaf(c.m3_s, ta + tb, r);
+    if (G == SPH) r = fmaf(c.m3_n, ua + ub, r);
+    return r;
+}
+
 // edge stress update from the sums of the 4 surrounding cells' ηSM and η with
 // gsc4 = GSDT/ηSM / 4: (τ + aG D) aE / (aE + aG), aG = gsc4 s4, aE = e4 / 4
 __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4, float e4, float D) {
@@ -404,7 +484,6 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     const bool s1_own = warp < FTY;
     const bool e12_xy = x < n1 - 1 && y < n2 - 1, e13_xy = x < n1 - 1 && y < n2 - 2, e23_xy = x < n1 - 2 && y < n2 - 1;
     const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
-    const EdgeMetric<float> em = edge_metric<float, G>(p.geo, x, y, n1, n2);
     const int gxy = x + d.sy * y;
     const bool y_face = y == 0 || y == n2 - 1;  // stage-1 point on an x2 face of the box
     const int iin = b * TIN_X + a + 3;   // input-tile index of the stage-1 point
@@ -413,7 +492,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     const int I = x0 + tx, J = y0 + ty;
     const bool v_ok = warp < FTY && I >= 1 && J >= 1 && I <= n1 - 1 && J <= n2 - 1;
     const bool m1_xy = J <= n2 - 2, m2_xy = I <= n1 - 2, m3_xy = I <= n1 - 2 && J <= n2 - 2;
-    const MomMetric<float> mm = mom_metric<float, G>(p.geo, I, J, n1, n2);
+    const SweepCoef sc = sweep_coef<G>(edge_metric<float, G>(p.geo, x, y, n1, n2), mom_metric<float, G>(p.geo, I, J, n1, n2), d2, d3);
     const int gIJ = I + d.sy * J;
 
     // this thread's stage-1 point of the current plane, and carried values of the previous plane
@@ -458,17 +537,17 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             vdt = pdiv(vpdt2, kb + gs * f);
         }
         {
-            const float D = edge12_m<float, G>(em, d1, d2, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
+            const float D = sw_edge12<G>(sc, d1, in1(1, 1, 0), in1(1, 1, 1), in1(0, 0, 1), in1(0, 1, 1));
             v12 = edge_update_q(old(I12), gsc4, in1(4, 0, 0) + in1(4, 1, 0) + in1(4, 0, 1) + in1(4, 1, 1),
                                 in1(3, 0, 0) + in1(3, 1, 0) + in1(3, 0, 1) + in1(3, 1, 1), D);
         }
         {
-            const float D = edge13_m<float, G>(em, d1, d3, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
+            const float D = sw_edge13<G>(sc, d1, in1(2, 1, 0), in1(2, 1, 1), in0(0, 1, 1), in1(0, 1, 1));
             v13 = edge_update_q(old(I13), gsc4, in0(4, 1, 0) + in1(4, 1, 0) + in0(4, 1, 1) + in1(4, 1, 1),
                                 in0(3, 1, 0) + in1(3, 1, 0) + in0(3, 1, 1) + in1(3, 1, 1), D);
         }
         {
-            const float D = edge23_m<float, G>(em, d2, d3, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
+            const float D = sw_edge23<G>(sc, in1(2, 0, 1), in1(2, 1, 1), in0(1, 1, 1), in1(1, 1, 1));
             v23 = edge_update_q(old(I23), gsc4, in0(4, 0, 1) + in1(4, 0, 1) + in0(4, 1, 1) + in1(4, 1, 1),
                                 in0(3, 0, 1) + in1(3, 0, 1) + in0(3, 1, 1) + in1(3, 1, 1), D);
         }
@@ -501,13 +580,13 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             const float h = 0.5f;
             const float t12a = C1[E12][ty + 1][tx], t12b = C1[E12][ty][tx];
             // V1 (I-1/2, J, K), cell m = (I-1, J, K)
-            float r1 = mom1_m<float, G>(mm, d1, d2, d3, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
+            float r1 = sw_mom1<G>(sc, d1, C0[Q11][ty + 1][tx], o11, C0[Q22][ty + 1][tx], o22, C0[Q33][ty + 1][tx], o33,
                                         t12a, t12b, c13, p13);
             // V2 (I, J-1/2, K), cell m = (I, J-1, K)
-            float r2 = mom2_m<float, G>(mm, d1, d2, d3, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
+            float r2 = sw_mom2<G>(sc, d1, C0[Q22][ty][tx + 1], o22, C0[Q33][ty][tx + 1], o33, C1[E12][ty][tx + 1], t12b,
                                         c23, p23);
             // V3 (I, J, K-1/2), cell m = (I, J, K-1)
-            float r3 = mom3_m<float, G>(mm, d1, d2, d3, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
+            float r3 = sw_mom3<G>(sc, d1, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
             if (MODE == 1) {
                 r1 += S.rv[K & 1][0][ty * FTX + tx];
                 r2 += S.rv[K & 1][1][ty * FTX + tx];

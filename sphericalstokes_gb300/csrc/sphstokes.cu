@@ -101,6 +101,11 @@ struct Ctx {
     cudaGraphExec_t corr_graph[2] = {nullptr, nullptr};
     float* corr_graph_key[2] = {nullptr, nullptr};   // F_P pointer at capture time
     int graph_len = 0;
+    // CUDA graphs of `warm_len` FP32 nonlinear iterations (mixed solve warm start), one per
+    // arrangement of the ping-pong and η buffers, keyed by the P and η pointers at capture
+    cudaGraphExec_t warm_graph[2] = {nullptr, nullptr};
+    float* warm_key[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
+    int warm_len = 0;
     bool use_graphs = true;
     // TMA tensor maps of the correction sweep, one set per ping-pong arrangement
     CUtensorMap* d_maps = nullptr;       // [2][TM_COUNT] in device memory
@@ -968,6 +973,58 @@ int apply_correction(Ctx& c) {
     return SPH_OK;
 }
 
+// the captured launches of a context (correction sweeps, warm-start iterations): dropped
+// when the launch parameters they hold change
+void drop_graphs(Ctx& c) {
+    for (int i = 0; i < 2; ++i) {
+        if (c.corr_graph[i]) cudaGraphExecDestroy(c.corr_graph[i]);
+        c.corr_graph[i] = nullptr;
+        c.corr_graph_key[i] = nullptr;
+        if (c.warm_graph[i]) cudaGraphExecDestroy(c.warm_graph[i]);
+        c.warm_graph[i] = nullptr;
+        c.warm_key[i][0] = c.warm_key[i][1] = nullptr;
+    }
+    c.graph_len = 0;
+    c.warm_len = 0;
+}
+
+// n (even, >= 8) FP32 nonlinear iterations of the warm start as one graph launch; after an
+// even count the ping-pong and η buffers are back in the arrangement the graph was captured in
+template <int G>
+int run_warm_iterations(Ctx& c, int n) {
+    if (n != c.warm_len) {
+        for (int i = 0; i < 2; ++i) {
+            if (c.warm_graph[i]) cudaGraphExecDestroy(c.warm_graph[i]);
+            c.warm_graph[i] = nullptr;
+            c.warm_key[i][0] = c.warm_key[i][1] = nullptr;
+        }
+        c.warm_len = n;
+    }
+    float* kp = c.s32.f[F_P];
+    float* ke = c.s32.f[F_ETA];
+    int slot = -1;
+    for (int i = 0; i < 2; ++i)
+        if (c.warm_graph[i] && c.warm_key[i][0] == kp && c.warm_key[i][1] == ke) slot = i;
+    if (slot < 0) {
+        slot = c.warm_graph[0] ? 1 : 0;
+        if (c.warm_graph[slot]) { cudaGraphExecDestroy(c.warm_graph[slot]); c.warm_graph[slot] = nullptr; }
+        CK(cudaStreamSynchronize(c.stream));
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < n; ++i) iterate_dispatch<float>(c, c.s32);  // recorded, not run
+        cudaError_t e = cudaStreamEndCapture(c.stream, &g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c.warm_graph[slot], g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+        c.warm_key[slot][0] = kp;
+        c.warm_key[slot][1] = ke;
+        if (c.s32.f[F_P] != kp || c.s32.f[F_ETA] != ke) return fail(SPH_ERR_UNSUPPORTED, "warm-start graph: buffer arrangement not restored");
+    }
+    CK(cudaGraphLaunch(c.warm_graph[slot], c.stream));
+    return SPH_OK;
+}
+
 template <int G>
 int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t* hi, double* he, int64_t cap) {
     State<double>& s = c.s64;
@@ -986,6 +1043,15 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
         if (rc) return rc;
         double werr = 1.0;
         while (iters < o.maxiter) {
+            // the plain iterations up to the next check, replayed from a graph
+            const int64_t before = nout - 1 - (iters % nout);
+            if (c.use_graphs && before >= 8 && iters + before < o.maxiter) {
+                const int n = (int)(before & ~int64_t(1));
+                rc = run_warm_iterations<G>(c, n);
+                if (rc) return rc;
+                iters += n;
+                continue;
+            }
             ++iters;
             const bool check = (iters % nout) == 0;
             if (check) { rc = snapshot<float>(c, t); if (rc) return rc; }
@@ -1292,12 +1358,7 @@ int sph_autotune(void* h, int32_t sweeps, int32_t* best_chunk, double* best_ms) 
     }
     if ((rc = check_kernel_flag(*c))) return rc;
     c->fused_chunk = bk;
-    for (int i = 0; i < 2; ++i) {  // graphs were captured with the previous chunk length
-        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
-        c->corr_graph[i] = nullptr;
-        c->corr_graph_key[i] = nullptr;
-    }
-    c->graph_len = 0;
+    drop_graphs(*c);  // graphs were captured with the previous chunk length
     {
         std::lock_guard<std::mutex> lock(g_tune_mu);
         g_tuned_chunk[std::make_tuple(c->prm.geometry, c->d.n1, c->d.n2, c->d.n3)] = bk;
@@ -1324,12 +1385,7 @@ int sph_update_params(void* h, const sph_params* p) {
     c->prm = n;
     c->cur_n = n.n_exp;
     // captured launches and the prepared correction problem hold the old scalars
-    for (int i = 0; i < 2; ++i) {
-        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
-        c->corr_graph[i] = nullptr;
-        c->corr_graph_key[i] = nullptr;
-    }
-    c->graph_len = 0;
+    drop_graphs(*c);
     c->corr_ready = false;
     if ((rc = build_bc(*c))) return rc;
     return compute_f_scale(*c);
@@ -1348,8 +1404,7 @@ int sph_destroy(void* h) {
     if (c->hred) cudaFreeHost(c->hred);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
-    for (int i = 0; i < 2; ++i)
-        if (c->corr_graph[i]) cudaGraphExecDestroy(c->corr_graph[i]);
+    drop_graphs(*c);
     if (c->ev2) cudaEventDestroy(c->ev2);
     if (c->ev3) cudaEventDestroy(c->ev3);
     if (c->ev4) cudaEventDestroy(c->ev4);

@@ -297,3 +297,19 @@ def test_sweep_two_points_per_thread_equals_one(monkeypatch, geom, n, kw):
             out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P")})
     for f in out[0]:
         assert relerr(out[1][f], out[0][f]) < 1e-5, f
+
+
+def test_warm_start_graph_equals_plain_iterations(monkeypatch):
+    """the mixed solve's FP32 warm start replayed from CUDA graphs gives what the iterations
+    launched one by one give (same iterations, same solution)"""
+    from bench import workload_params
+    out = []
+    for graphs in ("0", "1"):
+        monkeypatch.setenv("SPH_NO_GRAPHS", "1" if graphs == "0" else "0")
+        with S.Solver(workload_params(31, "mixed", tuned=True)) as sv:
+            r = sv.solve(tol=1e-8, maxiter=6000, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=3,
+                         inner_max=2000, warm_tol=1e-5)
+            out.append((r.iters, r.outer, r.residual, {f: sv.get(f) for f in ("V1", "V2", "V3", "P")}))
+    assert out[0][:3] == out[1][:3]
+    for f in out[0][3]:
+        assert np.array_equal(out[1][3][f], out[0][3][f]), f

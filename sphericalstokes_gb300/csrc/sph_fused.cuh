@@ -31,6 +31,11 @@ namespace sph {
 template <typename T>
 struct FusedOut {
     T *P, *V1, *V2, *V3, *t11, *t22, *t33, *t12, *t13, *t23;
+    // k_fused_tma only: ghost velocities on the two x1 faces written with the new values,
+    // ghost = xg[f] x (its interior neighbour) for the fields f of bit f in xg_mask (the
+    // first stage of the homogeneous BC program, which the launch then skips)
+    int xg_mask;
+    T xg[3];
 };
 
 constexpr int FTX = 32, FTY = 8;                  // owned tile (cells) per block
@@ -593,9 +598,21 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
                 r3 += S.rv[K & 1][2][ty * FTX + tx];
             }
             const bool kin = IN || K <= n3 - 2;
-            if (v_ok && m1_xy && kin) st_at(o.V1, gb, ov1 + r1 * ((C0[QDT][ty + 1][tx] + odt) * h));
-            if (v_ok && m2_xy && kin) st_at(o.V2, gb, ov2 + r2 * ((C0[QDT][ty][tx + 1] + odt) * h));
-            if (v_ok && m3_xy) st_at(o.V3, gb, ov3 + r3 * ((pdt + odt) * h));
+            const float v1 = ov1 + r1 * ((C0[QDT][ty + 1][tx] + odt) * h);
+            const float v2 = ov2 + r2 * ((C0[QDT][ty][tx + 1] + odt) * h);
+            const float v3 = ov3 + r3 * ((pdt + odt) * h);
+            if (v_ok && m1_xy && kin) {
+                st_at(o.V1, gb, v1);
+                if ((o.xg_mask & 1) && (I == 1 || I == n1 - 1)) st_at(o.V1, I == 1 ? gb - 4u : gb + 4u, o.xg[0] * v1);
+            }
+            if (v_ok && m2_xy && kin) {
+                st_at(o.V2, gb, v2);
+                if ((o.xg_mask & 2) && (I == 1 || I == n1 - 2)) st_at(o.V2, I == 1 ? gb - 4u : gb + 4u, o.xg[1] * v2);
+            }
+            if (v_ok && m3_xy) {
+                st_at(o.V3, gb, v3);
+                if ((o.xg_mask & 4) && (I == 1 || I == n1 - 2)) st_at(o.V3, I == 1 ? gb - 4u : gb + 4u, o.xg[2] * v3);
+            }
         }
         p13 = c13; p23 = c23; p33 = o33; pdt = odt;
     };

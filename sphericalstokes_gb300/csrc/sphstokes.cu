@@ -89,6 +89,11 @@ struct Ctx {
     unsigned long long* hred = nullptr;  // pinned host copy
     std::vector<BcStage> bc;      // BC program: ghost-velocity stages in the reference order (the adjoint transposes these)
     std::vector<BcStage> bc_run;  // the program launched by launch_bc: bc, or an equivalent one with fewer stages
+    // the first stage of bc_run in the homogeneous case as factors of the interior neighbour
+    // (ghost = xg[f] x neighbour on both x1 faces, field f in bit f of xg_mask); 0: not of that form
+    int xg_mask = 0;
+    float xg[3] = {0.f, 0.f, 0.f};
+    bool xg_fuse = true;  // the correction sweep writes those ghosts (SPH_NO_XGHOST=1: the BC stage does)
     double cur_n = 1.0;
     double f_scale = 1.0;
     double last_ms = 0.0;
@@ -230,8 +235,30 @@ BcStage stage(int dim, std::initializer_list<BcOp> ops) {
 int build_bc_program(Ctx& c);
 int build_bc(Ctx& c) {
     const int rc = build_bc_program(c);
-    if (rc == SPH_OK && c.bc_run.empty()) c.bc_run = c.bc;
-    return rc;
+    if (rc != SPH_OK) return rc;
+    if (c.bc_run.empty()) c.bc_run = c.bc;
+    // homogeneous x1-face stage as factors (NEG -1, COPY +1, ZERO / LIN 0, LIN2M -1)
+    c.xg_mask = 0;
+    const BcStage& s0 = c.bc_run[0];
+    int mask = 0;
+    float xg[3] = {0.f, 0.f, 0.f};
+    bool ok = s0.dim == 0 && c.xg_fuse;
+    for (int i = 0; ok && i < s0.nops; ++i) {
+        const BcOp& op = s0.op[i];
+        if (op.field < 0 || op.field > 2 || (mask >> op.field & 1)) { ok = false; break; }
+        switch (op.kind) {
+            case BC_NEG: case BC_LIN2M: xg[op.field] = -1.f; break;
+            case BC_COPY: xg[op.field] = 1.f; break;
+            case BC_ZERO: case BC_LIN: xg[op.field] = 0.f; break;
+            default: ok = false;
+        }
+        mask |= 1 << op.field;
+    }
+    if (ok && mask) {
+        c.xg_mask = mask;
+        for (int i = 0; i < 3; ++i) c.xg[i] = xg[i];
+    }
+    return SPH_OK;
 }
 
 // the ghost-velocity stages of the BC set (Julia reference order), in c.bc; a
@@ -285,8 +312,9 @@ int build_bc_program(Ctx& c) {
 }
 
 template <typename T, int G>
-void launch_bc(Ctx& c, KP<T>& p, int homog) {
-    for (const BcStage& st : c.bc_run) {
+void launch_bc(Ctx& c, KP<T>& p, int homog, int first = 0) {
+    for (size_t i = first; i < c.bc_run.size(); ++i) {
+        const BcStage& st = c.bc_run[i];
         int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1;
         int ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
         dim3 g((eu + 31) / 32, (ev + 7) / 8, 1);
@@ -887,12 +915,20 @@ template <int G>
 void correction_sweep(Ctx& c) {
     State<float>& t = c.s32;
     KP<float> q = make_kp_corr(c);
+    int first_bc = 0;
     if (c.fused) {
         const CUtensorMap* maps = tma_maps(c);
         if (maps) {
             FusedOut<float> o;
             o.P = t.f[F_A_P]; o.V1 = t.f[F_A_V1]; o.V2 = t.f[F_A_V2]; o.V3 = t.f[F_A_V3];
             o.t11 = t.f[F_A_T11]; o.t22 = t.f[F_A_T22]; o.t33 = t.f[F_A_T33]; o.t12 = t.f[F_A_T12]; o.t13 = t.f[F_A_T13]; o.t23 = t.f[F_A_T23];
+            o.xg_mask = 0;
+            o.xg[0] = o.xg[1] = o.xg[2] = 0.f;
+            if (!c.use_x2 && c.xg_mask) {  // the sweep writes the x1-face ghosts: the BC launch skips its first stage
+                o.xg_mask = c.xg_mask;
+                for (int i = 0; i < 3; ++i) o.xg[i] = c.xg[i];
+                first_bc = 1;
+            }
             const int kc = fused_chunk(c);
             dim3 grid((c.d.n1 + FTX - 1) / FTX, (c.d.n2 + FTY - 1) / FTY, (c.d.n3 + kc - 1) / kc);
             const bool prof = c.prof_on && 2 * c.prof_next + 1 < c.prof_ev.size();
@@ -914,7 +950,7 @@ void correction_sweep(Ctx& c) {
         k_stress<float, G, true><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(q);
         k_velocity<float, G, 1><<<grid_vel(c.d), blk2d(), 0, c.stream>>>(q);
     }
-    launch_bc<float, G>(c, q, 1);
+    launch_bc<float, G>(c, q, 1, first_bc);
 }
 
 // run `n` correction sweeps; with graphs enabled and n even, replays a captured
@@ -1282,6 +1318,7 @@ int sph_create(const sph_params* prm, void** out) {
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
     if (const char* e = std::getenv("SPH_NO_PDL")) c->use_pdl = std::atoi(e) == 0;
+    if (const char* e = std::getenv("SPH_NO_XGHOST")) c->xg_fuse = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
     if ((rc = init_fields(*c))) return cleanup(rc);
     if ((rc = compute_f_scale(*c))) return cleanup(rc);

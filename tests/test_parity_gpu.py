@@ -313,3 +313,23 @@ def test_warm_start_graph_equals_plain_iterations(monkeypatch):
     assert out[0][:3] == out[1][:3]
     for f in out[0][3]:
         assert np.array_equal(out[1][3][f], out[0][3][f]), f
+
+
+@pytest.mark.parametrize("geom,bc,n", [("spherical", "stress", (40, 17, 23)), ("spherical", "free_slip", 21),
+                                       ("spherical", "diapir", (33, 12, 19)), ("cylindrical", "diapir", (19, 33, 12)),
+                                       ("cartesian", "diapir", (35, 14, 27)), ("cylindrical", "stress", (23, 21, 17))])
+def test_sweep_x1_ghosts_equal_bc_stage(monkeypatch, geom, bc, n):
+    """the correction sweep writing the x1-face ghost velocities itself (and the BC launch
+    skipping that stage) leaves exactly the state the separate BC stage leaves"""
+    out = []
+    for off in ("1", "0"):
+        monkeypatch.setenv("SPH_NO_XGHOST", off)
+        p = S.default_params(geom, n1=n if isinstance(n, int) else n[0], n2=n if isinstance(n, int) else n[1],
+                             n3=n if isinstance(n, int) else n[2], n_exp=3.0, bc=bc, precision="mixed",
+                             rheology="edot_power_relax" if bc == "stress" else "linear")
+        with S.Solver(p) as sv:
+            sv.sweep(38)
+            sv.sweep_apply()
+            out.append({f: sv.get(f) for f in ("V1", "V2", "V3", "P", "TAU12", "TAU23")})
+    for f in out[0]:
+        assert np.array_equal(out[1][f], out[0][f]), f

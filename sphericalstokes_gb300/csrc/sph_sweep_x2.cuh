@@ -75,13 +75,15 @@ __device__ __forceinline__ MomMetric<F2> mom_metric_pair(const Geo<float>& geo, 
     return m;
 }
 
-// 8-byte store of a pair when both lanes are wanted, else lane by lane
-__device__ __forceinline__ void store_pair(float* base, long long g, F2 v, bool m0, bool m1) {
+// 8-byte store of a pair when both lanes are wanted, else lane by lane; `off` is the
+// 32-bit unsigned byte offset of the first point from the field's base
+__device__ __forceinline__ void store_pair(float* base, unsigned off, F2 v, bool m0, bool m1) {
+    char* q = reinterpret_cast<char*>(base) + off;
     if (m0 && m1) {
-        *reinterpret_cast<float2*>(base + g) = v.v;
+        *reinterpret_cast<float2*>(q) = v.v;
     } else {
-        if (m0) base[g] = v.v.x;
-        if (m1) base[g + 1] = v.v.y;
+        if (m0) *reinterpret_cast<float*>(q) = v.v.x;
+        if (m1) *reinterpret_cast<float*>(q + 4) = v.v.y;
     }
 }
 
@@ -152,7 +154,7 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
     const bool e23_0 = x < n1 - 2 && y < n2 - 1, e23_1 = x + 1 < n1 - 2 && y < n2 - 1;
     const CellMetric<F2> cm = cell_metric_pair<G>(p.geo, p.d2, p.d3, x, y, n1, n2);
     const EdgeMetric<F2> em = edge_metric_pair<G>(p.geo, x, y, n1, n2);
-    const long long gxy = x + (long long)d.sy * y;
+    const int gxy = x + d.sy * y;
     const int iin = b * TIN_X + a + 3;       // input-tile offset of the first point (even)
     const int iold = b * TOLD_X + a + 3;     // old-tile offset (even)
     const int ist = b * X2_SROW + a + 1;     // stress-ring offset (even)
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
         const float* O = &S.old[k & 1][0][0] + iold;
         auto old = [&](int f) { return F2(*reinterpret_cast<const float2*>(O + f * TOLD_TILE)); };
         const bool own = own_plane && main_warp;
-        const long long g = gxy + (long long)d.sz * k;
+        const unsigned g = 4u * (unsigned)(gxy + d.sz * k);  // byte offset (stored points only: >= 0)
         F2 vP(0.f), v11(0.f), v22(0.f), v33(0.f), vdt(0.f), v12(0.f), v13(0.f), v23(0.f);
         if (in0 || in1) {
             {
@@ -271,7 +273,7 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
         if (K == kA) { p13 = pairU(C1, E13, 0); p23 = pairU(C1, E23, 0); }
         const F2 c13 = pairU(C0, E13, 0), c23 = pairU(C0, E23, 0);
         if ((v0 || v1) && K >= 1 && K <= n3 - 1) {
-            const long long g = gxy + (long long)d.sz * K;  // node I = x, J = y
+            const unsigned g = 4u * (unsigned)(gxy + d.sz * K);  // byte offset of node I = x, J = y
             const F2 h(0.5f);
             const F2 t12a = F2(C1[E12 * RS + rOwn - 1], pe12);  // τ12 at (a-1, b), (a, b) of plane K-1
             const F2 t12b = pairU(C1, E12, 0);                   // τ12 at (a-1, b-1), (a, b-1)
@@ -307,29 +309,39 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
         issue_inputs(kA + 1);
         issue_old(kA);
     }
-    wait_in(kA - 1);
-    wait_in(kA);
-    wait_old(kA - 1);
+    // warp 0 alone waits on the mbarriers; the block barrier after its wait passes the landed
+    // copies on to the other warps
+    const bool waiter = warp == 0;
+    if (waiter) {
+        wait_in(kA - 1);
+        wait_in(kA);
+        wait_old(kA - 1);
+    }
+    __syncthreads();
     if (kA >= 1) {
         stage1(kA - 1, false);
         p33 = o33; pdt = odt; pe12 = o12; pe23 = o23;
     }
     for (int K = kA; K < kB; ++K) {
-        __syncthreads();  // every thread is done with the slots of plane K-1
+        if (waiter) {
+            wait_in(K + 1);
+            wait_old(K);
+        }
+        __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
         if (tid == 0) {
             issue_inputs(K + 2);
             issue_old(K + 1);
         }
-        wait_in(K + 1);
-        wait_old(K);
         stage1(K, true);
         __syncthreads();
         velocity(K);
     }
     // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
-    wait_in(kB + 1);
-    wait_old(kB);
-    if (!ok && err) atomicExch(err, 1);
+    if (waiter) {
+        wait_in(kB + 1);
+        wait_old(kB);
+        if (!ok && err) atomicExch(err, 1);
+    }
 }
 
 }  // namespace sph

@@ -644,9 +644,9 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             wait_old(K);
         }
         __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
-        if (tid == 0) {
-            issue_inputs(K + 2);
-            issue_old(K + 1);
+        if (tid == 0) {  // only planes the chunk uses: inputs up to kB, old state and rV up to kB - 1
+            if (K + 2 <= kB) issue_inputs(K + 2);
+            if (K + 1 <= kB - 1) issue_old(K + 1);
         }
         sk = sk == 2 ? 0 : sk + 1;
         stage1(K, true, sk, inner);
@@ -658,12 +658,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         if (K <= n3 - 3) step(K, std::true_type{});
         else step(K, std::false_type{});
     }
-    // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
-    if (waiter) {
-        wait_in(kB + 1);
-        wait_old(kB);
-        if (!ok && err) atomicExch(err, 1);
-    }
+    if (waiter && !ok && err) atomicExch(err, 1);  // every issued copy has been waited for: none is in flight
 }
 
 inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }

@@ -16,8 +16,10 @@
 // Every state field is read once and written once per sweep (halo re-reads
 // hit L2); the old and new states are different buffers (ping-pong) and the
 // boundary-condition stages run afterwards on the new state.  The arithmetic
-// is the shared core of sph_core.cuh: results equal those of k_stress +
-// k_velocity.
+// of k_fused is the shared core of sph_core.cuh: results equal those of
+// k_stress + k_velocity.  k_fused_tma (below) feeds the same march by TMA and
+// evaluates the edge-strain and momentum terms on per-thread coefficients
+// (SweepCoef): the same values up to FP32 rounding.
 //
 // MODE 0: reference iteration (ρg body force).  MODE 1: correction problem of
 // the mixed-precision solve (right-hand sides rP, rV; η and ηSM frozen).
@@ -418,7 +420,19 @@ __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4,
 
 // Waiting: warp 0 alone waits on the mbarriers of the planes a step needs and
 // the block barrier that follows passes the completed copies on to the other
-// warps, so nine of ten warps never poll.
+// warps, so nine of ten warps never poll.  A chunk copies only the planes it
+// uses (inputs kA-1 .. kB, old state and rV kA-1 .. kB-1), so nothing is in
+// flight when the march ends.
+//
+// Per-plane work is kept free of per-thread branching, which this kernel pays
+// for in issue slots (it is instruction-bound): every stage-1 thread evaluates
+// the cell and all three edges and every row thread all three velocity updates
+// (the tiles hold finite or zero-filled values outside the box); validity masks
+// only the stores and the stress-ring writes.  Planes 1 .. n3-3 run a body
+// without the x3 conditions.  Stores take 32-bit unsigned byte offsets.  The
+// x1-face ghost velocities of the homogeneous BC program's first stage are
+// written here with the new values (FusedOut::xg_mask), so that stage is not
+// launched.
 //
 // Thread roles (10 warps): warp w < 8 owns the row J = y0 + w of the tile, lane
 // l the column I = x0 + l: it computes the stage-1 point (I, J) (a = l+1,

@@ -14,9 +14,11 @@ dataset).
   FP32 PT sweeps of the FP32+FP64 defect-correction solve, inputs resident in
   HBM, device time from CUDA events on the library's stream.  One "step" is
   one PT sweep.
-* ``e2e``: the same metric through the C ABI with host buffers: upload of the
-  problem (ρ, η_ini, phase, V, P from pinned host memory), the whole mixed-
-  precision solve to FP64 residual 1e-8, download of V and P.
+* ``e2e``: the same metric through the C ABI with host buffers, per step of
+  K sweeps: upload of the problem (ρ, η_ini, η, phase, V, P from pinned host
+  memory), one defect-correction step of the mixed-precision solve (FP64
+  residual, K FP32 sweeps, FP64 update and residual), download of V and P
+  into pinned host memory.
 * ``roofline``: the fused sweep kernel alone — A_eff per launch over its average
   launch duration, from CUDA event pairs around each launch on the library's
   stream (``sph_sweep_profile``, the same K sweeps launched one at a time).
@@ -24,6 +26,11 @@ dataset).
   plain FP64 PT on the same workload at ``--solve-n`` cells per axis (default
   63: plain FP64 PT at 255^3 runs for hours), with the relative velocity error
   of the mixed solution against the FP64 one.
+* ``batch``: a seeded draw of small uneven solves (``--batch``, edges from
+  ``--batch-edges``) through ``sph_batch_solve`` against the same solves one
+  after another.
+* ``plateau_511x255x255``: FP32 correction sweeps of the elliptical plateau
+  set-up on its 511 x 255 x 255 grid (``--plateau-sweeps``).
 * ``cpu_baseline``: the FP64 CPU oracle (restatement of the reference kernels)
   timed on the host cores on a bounded sample of the same workload.
 

@@ -531,8 +531,9 @@ std::map<std::tuple<int, int, int, int>, int> g_tuned_chunk;
 // chunk and the pipeline fill), while the hardware scheduler balances the SMs
 // only to within one block at the end of the launch.  The time model
 // (k + 2.5) * (blocks / slots + 0.7), slots = resident blocks on the device, picks
-// the chunk among 4..24 planes; at 63^3, 127^3 and 255^3 its pick is within
-// 1 % of the fastest chunk measured on a GB300 (sph_autotune measures instead).
+// the chunk among 4..24 planes.  Measured on a GB300, its pick is the fastest
+// chunk at 63^3 and within 1 % of it at 255^3 and 5 % at 127^3, where wave
+// quantisation makes the ranking irregular (sph_autotune measures instead).
 int fused_chunk(const Ctx& c) {
     if (c.fused_chunk > 0) return c.fused_chunk;
     const double xy = (double)((c.d.n1 + FTX - 1) / FTX) * ((c.d.n2 + FTY - 1) / FTY);

@@ -279,7 +279,7 @@ def run_ours(args) -> None:
         prof_sweep_ms, prof_kernel_ms = sv.sweep_profile(args.steps)
     value = aeff * world / (ms_step_max * 1e-3) / 1e9
     kernel_ms = prof_kernel_ms / max(args.steps, 1)
-    launches_per_sweep = 1 + 3  # fused sweep + the three launched stages of the stress BC set
+    launches_per_sweep = 1 + 2  # fused sweep (writes the x1-face ghosts) + the x2- and x3-face stages of the stress BC set
     out.update({"value": round(value, 3), "ms_per_step": round(ms_step_max, 5), "kernel_ms": kernel_ms,
                 "kernel_share": prof_kernel_ms / prof_sweep_ms if prof_sweep_ms > 0 else None})
 

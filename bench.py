@@ -76,6 +76,38 @@ def workload_desc(n: int) -> str:
             f"(relax 0.5) + linear inclusion η=1e-3 Δρ=-1 r=0.1, far-field σθθ=+0.5 σφφ=-0.5")
 
 
+def workload_config(n: int) -> dict:
+    """The ``config`` of both arms' lines (identical, so the two lines describe one workload)."""
+    return {"workload": workload_desc(n), "n": n,
+            "step": "one PT iteration over the workload's grid (T_eff from A_eff = 26 n^3 sizeof(T) per iteration)",
+            "l2": "state > 1.7 GB per iteration at 255^3 > L2 (inputs larger than L2, no flush)", "parallelism": "replicas"}
+
+
+def reference_params(n: int, m: int | None = None):
+    """The parameters of the n=3 workload built without the library: the values of
+    ``workload_params(n, "fp64")`` (spherical defaults of the diapir script with the sector
+    geometry), m x3 planes at the same spacing about the sector's centre (all n when m is None)."""
+    from types import SimpleNamespace
+
+    m = n if m is None else m
+    vr = 1e3
+    cfl = 1.0 / (2.0 + 4.5 * math.log10(vr))
+    hmin = min(1.0 / (n - 1), 0.5 * (math.pi / 2) / (n - 1), 0.5 * math.sin(math.pi / 4) * (math.pi / 2) / (n - 1))
+    p = SimpleNamespace(geometry=0, bc=2, rheology=3, init=1, n1=n, n2=n, n3=m, c1=1.0, c2=math.pi / 2, c3=0.0,
+                        l1=1.0, l2=math.pi / 2, l3=(math.pi / 2) * (m - 1) / (n - 1), l_ref=1.0, vpdt=hmin * cfl, dmp=4.5,
+                        g=1.0, tau_C=1.0, n_exp=3.0, relax=0.5, edot_bg=0.25, r=1.0, sh=0.0, sig_bc=(0.0, 0.5, -0.5),
+                        eta0=1.0, vr=vr, rho0=0.0, rho_in=-1.0, radius=0.01, incl_linear=1, etasm_passes=1)
+    return p
+
+
+def reference_workload(n: int, m: int | None = None):
+    """(parameters, oracle state) of the workload for the oracle port of the reference's kernels."""
+    import oracle
+
+    p = reference_params(n, m)
+    return p, oracle.Sph.from_params(p)
+
+
 # ---------------------------------------------------------------------------
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
@@ -144,8 +176,7 @@ def cpu_baseline(n: int, seconds: float = 15.0, threads: int | None = None) -> d
 
     if threads:
         oracle.set_threads(threads)
-    p = workload_params(n, "fp64")
-    o = oracle.Sph.from_params(p)
+    _, o = reference_workload(n)
     o.iterate(1)  # warm-up
     t0 = time.perf_counter()
     it = 0
@@ -170,10 +201,9 @@ def run_reference(args) -> None:
     if rank != 0:
         return
     import oracle
-    import sphericalstokes_gb300 as S
 
     n = args.n
-    full = oracle.Sph.from_params(workload_params(n, "fp64"))
+    _, full = reference_workload(n)
     full.iterate(1)
     t0 = time.perf_counter()
     full.iterate(1)
@@ -181,28 +211,99 @@ def run_reference(args) -> None:
     del full
     nsteps = args.steps + args.warmup
     m = int(max(8, min(n, math.floor(n * args.ref_seconds / max(nsteps * t_full, 1e-9)))))
-    p = workload_params(n, "fp64")
-    S.set_params(p, n3=m, l3=p.l3 * (m - 1) / (n - 1))  # same spacing, m planes
-    o = oracle.Sph.from_params(p)
+    _, o = reference_workload(n, m)  # same spacing, m x3 planes about the sector's centre
     for _ in range(args.warmup):
         o.iterate(1)
     t0 = time.perf_counter()
     for _ in range(args.steps):
         o.iterate(1)
     dt = (time.perf_counter() - t0) / max(args.steps, 1)
-    teff = S.teff_bytes(n, n, m, 8) / dt / 1e9
+    teff = 26.0 * n * n * m * 8 / dt / 1e9
+    ms_full = dt * 1e3 * n / m  # the sample's time per cell over the whole grid
     sample = (f"{args.steps} FP64 PT iterations on {n}x{n}x{m} cells ({m} x3 planes of the {n}^3 workload at its spacing; "
               f"one full {n}^3 iteration took {t_full * 1e3:.0f} ms)")
     line = {
         "metric": METRIC, "value": round(teff, 3), "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-        "config": {"workload": workload_desc(n), "n": n, "step": "one FP64 PT iteration over the grid sample (oracle port of the reference kernels)",
-                   "sample_planes": m},
+        "config": workload_config(n),
+        "ms_per_iteration": round(ms_full, 3), "word_bytes": 8,
         "cpu_baseline": {"value": round(teff, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": round(teff, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def _curve(ms: "np.ndarray", err: "np.ndarray", keep: int = 40) -> list:
+    """(seconds, residual) pairs of a solve's history, at most ``keep`` of them (the last kept)."""
+    import numpy as np
+
+    idx = np.unique(np.linspace(0, len(ms) - 1, min(keep, len(ms))).astype(int)) if len(ms) else []
+    return [[round(float(ms[i]) * 1e-3, 3), float(err[i])] for i in idx]
+
+
+def _time_to(ms, err, level: float):
+    """Seconds at the first history entry with residual <= level (None if never)."""
+    for t, e in zip(ms, err):
+        if e <= level:
+            return float(t) * 1e-3
+    return None
+
+
+def time_to_tolerance(args) -> dict:
+    """Mixed-precision solve to FP64 residual 1e-8 and plain FP64 PT from the same start with the same
+    PT parameters.  Plain FP64 runs to 1e-8 or for --fp64-budget-s seconds (iterations from a short
+    timed probe), with its residual history: the speed-up is taken at the residual both reached (1e-8
+    when both converged), from their residual-against-time curves."""
+    import numpy as np
+
+    import sphericalstokes_gb300 as S
+
+    n = args.solve_n
+    info: dict = {"n": n, "tol": 1e-8}
+    vel = {}
+    p = workload_params(n, "mixed", tuned=args.tuned)
+    with S.Solver(p) as sv:
+        r = sv.solve(tol=1e-8, maxiter=args.max_sweeps, nout=100, criterion="residual", inner_rtol=args.inner_rtol,
+                     max_outer=args.max_outer, inner_max=args.inner_max, warm_tol=args.warm_tol, hist_cap=1_000_000)
+        ms_m = sv.history_ms()
+        err_m = r.hist_err[:len(ms_m)]
+        vel["mixed"] = [sv.get(f) for f in ("V1", "V2", "V3")]
+    info["mixed"] = {"seconds": round(r.seconds, 3), "iterations": r.iters, "outer": r.outer, "residual": r.residual,
+                     "converged": r.converged, "sweep_s": round(r.sweep_ms * 1e-3, 3), "outer_s": round(r.outer_ms * 1e-3, 3),
+                     "curve_s_residual": _curve(ms_m, err_m)}
+    p = workload_params(n, "fp64", tuned=args.tuned)
+    nout = args.fp64_nout
+    maxiter = args.fp64_maxiter
+    if args.fp64_budget_s > 0:
+        with S.Solver(p) as probe:  # FP64 ms per iteration (a separate state: the solve below starts fresh)
+            probe.step(10)
+            ms_it = probe.step(50) / 50
+        maxiter = min(maxiter, max(nout, int(args.fp64_budget_s * 1e3 / ms_it) // nout * nout))
+        info["fp64_budget_s"] = args.fp64_budget_s
+    with S.Solver(p) as sv:
+        r = sv.solve(tol=1e-8, maxiter=maxiter, nout=nout, criterion="residual", hist_cap=1_000_000)
+        ms_f = sv.history_ms()
+        err_f = r.hist_err[:len(ms_f)]
+        vel["fp64"] = [sv.get(f) for f in ("V1", "V2", "V3")]
+    info["fp64"] = {"seconds": round(r.seconds, 3), "iterations": r.iters, "residual": r.residual, "converged": r.converged,
+                    "ms_per_iteration": round(r.device_ms / max(r.iters, 1), 4), "maxiter": maxiter,
+                    "curve_s_residual": _curve(ms_f, err_f)}
+    # the residual both solves reached: 1e-8 if plain FP64 converged, else its last (lowest) residual
+    common = max(1e-8, float(np.nanmin(err_f)) if len(err_f) else 1.0)
+    tm, tf = _time_to(ms_m, err_m, common), _time_to(ms_f, err_f, common)
+    info["common_residual"] = common
+    info["seconds_to_common_residual"] = {"mixed": tm, "fp64": tf}
+    if tm and tf:
+        info["speedup_mixed_vs_fp64"] = round(tf / tm, 2)
+    vmax = max(float(np.abs(v).max()) for v in vel["fp64"])
+    info["rel_velocity_error_mixed_vs_fp64"] = max(float(np.abs(a - b).max()) for a, b in zip(vel["mixed"], vel["fp64"])) / vmax
+    info["rel_velocity_error_against"] = ("the converged FP64 solution" if info["fp64"]["converged"]
+                                          else f"the last FP64 iterate (residual {info['fp64']['residual']:.2e})")
+    info["pt_parameters"] = ("ηSM max filter 2 passes, pseudo-step 2x the reference CFL, dmp 3 (both solves)" if args.tuned
+                             else "the reference's PT step (CFL = 1/(2+4.5 log10 vr) of the smallest spacing), dmp 4.5 (both solves)")
+    return info
 
 
 # ---------------------------------------------------------------------------
@@ -266,12 +367,21 @@ def run_ours(args) -> None:
             sv.solve(tol=1e-8, maxiter=args.prep_sweeps, nout=100, criterion="residual", inner_rtol=1e-3, max_outer=2,
                      inner_max=args.prep_sweeps)
         sv.sweep(args.warmup)
-        barrier()
+        # nvidia-smi samples every 200 ms and the K timed sweeps last a few ms at the default K, so
+        # the sampler runs over the same K-sweep block repeated for clock_load_s seconds before and
+        # half that after the timed region: its samples are of this load, the timed block included
         clk = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
         clk.start()
-        ms = sv.sweep(args.steps)
-        clocks = clk.stop()
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < args.clock_load_s:
+            sv.sweep(args.steps)
         barrier()
+        ms = sv.sweep(args.steps)
+        barrier()
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < 0.5 * args.clock_load_s:
+            sv.sweep(args.steps)
+        clocks = clk.stop()
         ms_step = ms / max(args.steps, 1)
         ms_step_max = max_over_ranks(ms_step)
         # the same K sweeps once more, launched one at a time with an event pair around every
@@ -323,25 +433,7 @@ def run_ours(args) -> None:
                        "download V and P into pinned host memory (one call chain)"}
 
     if args.solve_n:
-        vel = {}
-        for prec in ("mixed", "fp64"):
-            p = workload_params(args.solve_n, prec, tuned=True)
-            with S.Solver(p) as sv:
-                if prec == "mixed":
-                    r = sv.solve(tol=1e-8, maxiter=args.max_sweeps, nout=100, criterion="residual", inner_rtol=args.inner_rtol,
-                                 max_outer=args.max_outer, inner_max=args.inner_max, warm_tol=args.warm_tol)
-                else:
-                    r = sv.solve(tol=1e-8, maxiter=args.fp64_maxiter, nout=1000, criterion="residual")
-                vel[prec] = [sv.get(f) for f in ("V1", "V2", "V3")]
-                solve_info[prec] = {"n": args.solve_n, "seconds": round(r.seconds, 3), "iterations": r.iters,
-                                    "outer": r.outer, "residual": r.residual, "converged": r.converged}
-        vmax = max(float(np.abs(v).max()) for v in vel["fp64"])
-        solve_info["rel_velocity_error_mixed_vs_fp64"] = max(
-            float(np.abs(a - b).max()) for a, b in zip(vel["mixed"], vel["fp64"])) / vmax
-        solve_info["pt_parameters"] = "ηSM max filter 2 passes, pseudo-step 2x the reference CFL, dmp 3 (both solves)"
-        if solve_info["mixed"]["converged"] and solve_info["fp64"]["converged"]:
-            solve_info["speedup_mixed_vs_fp64"] = round(solve_info["fp64"]["seconds"] / solve_info["mixed"]["seconds"], 2)
-
+        solve_info = time_to_tolerance(args)
     plateau_info = None
     if args.plateau_sweeps > 0:
         from sphericalstokes_gb300 import plateau as PL
@@ -382,8 +474,9 @@ def run_ours(args) -> None:
         "metric": METRIC, "value": out["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": out["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "fp32 sweeps + fp64 residual/correction", "data": "synthetic",
-        "config": {"workload": workload_desc(n), "n": n, "step": "one FP32 PT sweep of the FP32+FP64 defect-correction solve",
-                   "l2": "state 1.7 GB per sweep > L2 (inputs larger than L2, no flush needed)", "parallelism": "replicas"},
+        "config": workload_config(n),
+        "ms_per_iteration": round(ms_step_max, 5), "word_bytes": word,
+        "iteration": "one FP32 PT sweep of the FP32+FP64 defect-correction solve",
         "roofline": {"bound": "hbm", "kernel": "k_fused_tma (FP32 PT sweep, correction problem)",
                      "achieved": round(aeff / (out["kernel_ms"] * 1e-3) / 1e9, 3), "peak": pk["hbm_gbs"], "unit": "GB/s",
                      "frac": round(aeff / (out["kernel_ms"] * 1e-3) / 1e9 / pk["hbm_gbs"], 4),
@@ -417,6 +510,11 @@ def main():
     ap.add_argument("--solve-n", type=int, default=63,
                     help="time mixed vs plain FP64 PT to residual 1e-8 at this size (0: skip; 255 takes hours in FP64)")
     ap.add_argument("--fp64-maxiter", type=int, default=2_000_000)
+    ap.add_argument("--fp64-budget-s", type=float, default=0.0,
+                    help="cap plain FP64 PT of the time-to-tolerance leg at about this many seconds (0: run to 1e-8)")
+    ap.add_argument("--fp64-nout", type=int, default=1000, help="FP64 residual checks every this many iterations")
+    ap.add_argument("--tuned", type=int, default=1,
+                    help="time-to-tolerance PT parameters: 1 the tuned set (2 ηSM passes, 2x step, dmp 3), 0 the reference's")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0, help="target length of the --impl reference run")
@@ -427,8 +525,12 @@ def main():
     ap.add_argument("--inner-max", type=int, default=200_000)
     ap.add_argument("--warm-tol", type=float, default=1e-3,
                     help="FP32 warm-start tolerance of the mixed solve (1e-3: shortest time at 63^3 among 1e-2 .. 1e-5)")
-    ap.add_argument("--traffic", type=float, default=1.76e9,
-                    help="ncu DRAM bytes per launch of the fused sweep at 255^3 (profiles/k_fused_tma_sph255_traffic.md)")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the fused sweep kernel, as an ncu capture of the same build measured "
+                         "them (dram__bytes_read.sum + dram__bytes_write.sum); reported as roofline.traffic (null if absent)")
+    ap.add_argument("--clock-load-s", type=float, default=1.0,
+                    help="seconds of the same sweep load before (and half of it after) the timed region, so that the "
+                         "200 ms clock sampler sees it")
     ap.add_argument("--batch", type=int, default=12, help="batched-solve leg: number of solves (0: skip)")
     ap.add_argument("--batch-edges", default="31,47", help="grid edges the batched solves draw from")
     ap.add_argument("--batch-budget", type=int, default=20000, help="sweep budget per batched solve")

@@ -228,6 +228,12 @@ int sph_step(void* ctx, int64_t k);
 int sph_solve(void* ctx, const sph_solve_opts* opts, sph_solve_info* info,
               int64_t* hist_iter, double* hist_err, int64_t hist_cap);
 
+/* Wall-clock milliseconds from the start of the last sph_solve on this context to each of its
+ * history entries (the (iter, err) pairs it wrote, in order; no counterpart in the reference,
+ * whose scripts print the error at each check): *n = number of entries, ms[0 .. min(cap, *n))
+ * filled.  For residual-against-time curves of a solve. */
+int sph_solve_history_ms(void* ctx, double* ms, int64_t cap, int64_t* n);
+
 /* MIXED only: k FP32 PT sweeps of the current defect-correction step (the hot path of
  * sph_solve).  The first call after the FP64 state changed prepares the step (FP64
  * residual, frozen viscosity, zero correction) outside the timed region;
@@ -235,6 +241,32 @@ int sph_solve(void* ctx, const sph_solve_opts* opts, sph_solve_info* info,
  * sph_sweep_apply() adds the correction to the FP64 state and ends the step. */
 int sph_sweep(void* ctx, int64_t k);
 int sph_sweep_apply(void* ctx);
+
+/* Fields of the correction problem that sph_sweep iterates (MIXED only; no counterpart in the
+ * reference: the FP32 state of the defect-correction step, for inspection and parity checks):
+ * the correction δP, δV1..δV3, δτ11..δτ23 (the sizes of P, V1..V3, τ11..τ23), the frozen
+ * viscosity η and ηSM (P's size) and the right-hand sides rP (P's size) and rV1..rV3 (the
+ * velocity arrays' sizes).  Values cross the boundary as doubles in the reference layout and
+ * are stored as FP32.  The first access after the FP64 state changed prepares the step as
+ * sph_sweep does (FP64 residual into rP/rV, η_eff into η, ηSM from it, zero correction);
+ * sph_corr_set then overwrites single fields of it, so a caller can pose its own correction
+ * problem; sph_sweep and sph_sweep_apply act on what is stored. */
+typedef enum sph_corr_field {
+    SPH_CORR_DP = 0, SPH_CORR_DV1 = 1, SPH_CORR_DV2 = 2, SPH_CORR_DV3 = 3,
+    SPH_CORR_DTAU11 = 4, SPH_CORR_DTAU22 = 5, SPH_CORR_DTAU33 = 6, SPH_CORR_DTAU12 = 7, SPH_CORR_DTAU13 = 8, SPH_CORR_DTAU23 = 9,
+    SPH_CORR_ETA = 10, SPH_CORR_ETA_SM = 11, SPH_CORR_RP = 12, SPH_CORR_RV1 = 13, SPH_CORR_RV2 = 14, SPH_CORR_RV3 = 15,
+    SPH_CORR_COUNT = 16
+} sph_corr_field;
+int sph_corr_get(void* ctx, int32_t field, double* host, int64_t count);
+int sph_corr_set(void* ctx, int32_t field, const double* host, int64_t count);
+
+/* Self-test of the sweeps' failure path (no counterpart in the reference): launches on the
+ * context's stream a one-block kernel that waits, with the TMA sweeps' bounded wait cut to
+ * about a millisecond, on a barrier that nothing completes, and records the time-out in the
+ * context's error word as a sweep does.  Returns what a sweep call returns after such a
+ * time-out: SPH_ERR_CUDA, with the context marked unusable (every later call that launches
+ * work on it fails with SPH_ERR_CUDA; destroy it).  No copy or fault is involved. */
+int sph_selftest_wait_timeout(void* ctx);
 
 /* MIXED only (no counterpart in the reference: measurement): k sweeps as sph_sweep,
  * launched one at a time with a CUDA event pair on the library's stream around each
@@ -315,7 +347,9 @@ int sph_save(void* ctx, const char* dir, int32_t num, double tol, double runtime
  * It allocates no memory: its reduction slots are a static device array of
  * 2 * SPH_NOALLOC_MAX_ARRAYS * 8 bytes shared by every call, so calls that overlap on
  * the GPU race.  The first call on a device looks the array up (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture. */
+ * with that device current; make that first call before any stream capture.  The address
+ * is kept for the life of the process, so no call may follow a cudaDeviceReset of that
+ * device.  A NaN in v[i] or v_old[i] makes *err NaN (Julia's maximum propagates NaN). */
 #define SPH_NOALLOC_MAX_ARRAYS 8
 int sph_check_err_noalloc(int32_t m, const double* const* v, const double* const* v_old, const int64_t* count, double* err,
                           void* stream);

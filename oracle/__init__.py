@@ -204,6 +204,17 @@ class Sph:
     def apply_bc(self):
         lib().orc_sph_apply_bc(C.byref(self.st), C.byref(self.prm))
 
+    def corr_sweep(self, rP, rV1, rV2, rV3, k: int = 1):
+        """k correction sweeps of the mixed-precision solve (orc_sph_corr_sweep): the state holds the
+        correction (δP, δV, δτ), η and ηSM are frozen, rP / rV are the right-hand sides (reference layouts)."""
+        rhs = [np.asfortranarray(np.asarray(a, dtype=np.float64)) for a in (rP, rV1, rV2, rV3)]
+        for a, f in zip(rhs, ("P", "V1", "V2", "V3")):
+            if a.shape != self.field(f).shape:
+                raise ValueError(f"right-hand side of {f}: shape {a.shape}, expected {self.field(f).shape}")
+        L = lib()
+        L.orc_sph_corr_sweep.argtypes = [C.POINTER(SphState), C.POINTER(SphParams), _PD, _PD, _PD, _PD, C.c_int64]
+        L.orc_sph_corr_sweep(C.byref(self.st), C.byref(self.prm), *[_ptr(a) for a in rhs], int(k))
+
     def residual(self, f_scale: float | None = None) -> dict:
         nr, nt, np_ = self.n
         scr = np.zeros(int(lib().orc_sph_residual_scratch_size(nr, nt, np_)), dtype=np.float64)
@@ -283,6 +294,22 @@ class CC:
         return cls(geometry, fields, x1, x2, x3, d1=d[0], d2=d[1], d3=d[2], dmp=sc["dmp"], vpdt=sc["vpdt"], lr=lr,
                    g=sc["g"], tau_C=sc["τ_C"], n_exp=sc["n_exp"], relax=sc["relax"], r=sc.get("r", 0.0), sh=sc["sh"])
 
+    @classmethod
+    def from_params(cls, p) -> "CC":
+        """Zero state of a library ``Params`` of cylindrical (1) or Cartesian (2) geometry: node
+        coordinates c ± l/2, spacings l/(n-1), the scalars of the scripts."""
+        geometry = {1: "cylindrical", 2: "cartesian"}[p.geometry]
+        n1, n2, n3 = p.n1, p.n2, p.n3
+        z = lambda *s: np.zeros(s, dtype=np.float64, order="F")
+        fields = {f: z(n1, n2, n3) for f in ("P", "TAU11", "TAU22", "TAU33", "RHO", "ETA", "ETA_INI", "ETA_PL", "ETA_SM",
+                                             "DT_R", "TII")}
+        fields.update(V1=z(n1 + 1, n2, n3), V2=z(n1, n2 + 1, n3), V3=z(n1, n2, n3 + 1), TAU12=z(n1 - 1, n2 - 1, n3 - 2),
+                      TAU13=z(n1 - 1, n2 - 2, n3 - 1), TAU23=z(n1 - 2, n2 - 1, n3 - 1))
+        vpdt = p.vpdt if p.vpdt > 0 else p.l1 / (n1 - 1) / (2.0 + 4.5 * math.log10(p.vr))
+        return cls(geometry, fields, linspace(p.c1, p.l1, n1), linspace(p.c2, p.l2, n2), linspace(p.c3, p.l3, n3),
+                   d1=p.l1 / (n1 - 1), d2=p.l2 / (n2 - 1), d3=p.l3 / (n3 - 1), dmp=p.dmp, vpdt=vpdt, lr=p.l_ref, g=p.g,
+                   tau_C=p.tau_C, n_exp=p.n_exp, relax=p.relax, r=p.r, sh=p.sh)
+
     def field(self, name: str) -> np.ndarray:
         return self.arr[name]
 
@@ -290,6 +317,17 @@ class CC:
         fn = lib().orc_cyl_iterate if self.geometry == "cylindrical" else lib().orc_cart_iterate
         fn.argtypes = [C.POINTER(CCState), C.POINTER(CCParams), C.c_int64]
         fn(C.byref(self.st), C.byref(self.prm), int(k))
+
+    def corr_sweep(self, rP, rV1, rV2, rV3, k: int = 1):
+        """k correction sweeps of the mixed-precision solve (orc_cc_corr_sweep), as Sph.corr_sweep."""
+        rhs = [np.asfortranarray(np.asarray(a, dtype=np.float64)) for a in (rP, rV1, rV2, rV3)]
+        for a, f in zip(rhs, ("P", "V1", "V2", "V3")):
+            if a.shape != self.arr[f].shape:
+                raise ValueError(f"right-hand side of {f}: shape {a.shape}, expected {self.arr[f].shape}")
+        L = lib()
+        L.orc_cc_corr_sweep.argtypes = [C.c_int32, C.POINTER(CCState), C.POINTER(CCParams), _PD, _PD, _PD, _PD, C.c_int64]
+        L.orc_cc_corr_sweep(1 if self.geometry == "cylindrical" else 2, C.byref(self.st), C.byref(self.prm),
+                            *[_ptr(a) for a in rhs], int(k))
 
 
 def golden_fields(g, geometry: str, prefix: str) -> dict:

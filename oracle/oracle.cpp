@@ -148,8 +148,10 @@ void orc_sph_init_velocity(double* Vp, const double* th, int64_t nr, int64_t nt,
                 V(i, j, k) = (k <= np) ? (T(i, j, k) - PI / 2.0) * r * fact : (T(i, j, k - 1) - PI / 2.0) * r * fact;
 }
 
-// compute_P!  SphericalStokes_diapir.jl:155-241 (macros :155-208)
-void orc_sph_compute_P(orc_sph_state* s, const orc_sph_params* q) {
+// compute_P!  SphericalStokes_diapir.jl:155-241 (macros :155-208).  rP (EXT, may be NULL):
+// right-hand side of the continuity row of the correction problem, P -= KBDT (DIVV + rP);
+// the deviatoric strain rates use DIVV alone.
+static void sph_compute_P_impl(orc_sph_state* s, const orc_sph_params* q, const double* rP) {
     const long nr = s->nr, nt = s->nt, np = s->np;
     Arr P = A(s->P, nr, nt, np), DT_R = A(s->DT_R, nr, nt, np);
     Arr tRR = A(s->tRR, nr, nt, np), ttt = A(s->ttt, nr, nt, np), tpp = A(s->tpp, nr, nt, np);
@@ -174,7 +176,8 @@ void orc_sph_compute_P(orc_sph_state* s, const orc_sph_params* q) {
                 double Dpp = 1.0 / Rc / std::sin(tc) * (Vp(i, j, k + 1) - Vp(i, j, k)) * _dp + avxa_VR / Rc +
                              avya_Vt / Rc * cot(tc) - 1.0 / 3.0 * DIVV;
                 double kb = KBDT(i, j, k), gs = GSDT(i, j, k), e = eta(i, j, k);
-                P(i, j, k) = P(i, j, k) - kb * DIVV;
+                const double dv = rP ? DIVV + rP[(i - 1) + nr * ((j - 1) + nt * (k - 1))] : DIVV;
+                P(i, j, k) = P(i, j, k) - kb * dv;
                 tRR(i, j, k) = (tRR(i, j, k) + gs * 2.0 * DRR) / (1.0 + gs / e);
                 ttt(i, j, k) = (ttt(i, j, k) + gs * 2.0 * Dtt) / (1.0 + gs / e);
                 tpp(i, j, k) = (tpp(i, j, k) + gs * 2.0 * Dpp) / (1.0 + gs / e);
@@ -212,6 +215,8 @@ void orc_sph_compute_P(orc_sph_state* s, const orc_sph_params* q) {
             }
 }
 
+void orc_sph_compute_P(orc_sph_state* s, const orc_sph_params* q) { sph_compute_P_impl(s, q, nullptr); }
+
 // compute_TII!  SphericalStokes_diapir.jl:243-257 (interior only; faces via copy_BC!)
 void orc_sph_compute_TII(orc_sph_state* s) {
     const long nr = s->nr, nt = s->nt, np = s->np;
@@ -238,8 +243,10 @@ void orc_sph_power_law(orc_sph_state* s, const orc_sph_params* q) {
     }
 }
 
-// compute_V!  SphericalStokes_diapir.jl:267-329 (macros :267-307)
-void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) {
+// compute_V!  SphericalStokes_diapir.jl:267-329 (macros :267-307).  rV (EXT, may be NULL):
+// right-hand sides of the momentum rows of the correction problem (velocity-array
+// layouts), added to dV; the caller passes g = 0 with them.
+static void sph_compute_V_impl(orc_sph_state* s, const orc_sph_params* q, const double* const* rV) {
     const long nr = s->nr, nt = s->nt, np = s->np;
     Arr P = A(s->P, nr, nt, np), DT_R = A(s->DT_R, nr, nt, np), rho = A(s->rho, nr, nt, np);
     Arr tRR = A(s->tRR, nr, nt, np), ttt = A(s->ttt, nr, nt, np), tpp = A(s->tpp, nr, nt, np);
@@ -251,6 +258,8 @@ void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) {
     auto stt = [&](long i, long j, long k) { return -P(i, j, k) + ttt(i, j, k); };
     auto spp = [&](long i, long j, long k) { return -P(i, j, k) + tpp(i, j, k); };
     auto rG = [&](long i, long j, long k) { return rho(i, j, k) * g; };
+    Arr rV1 = A(rV ? const_cast<double*>(rV[0]) : nullptr, nr + 1, nt, np), rV2 = A(rV ? const_cast<double*>(rV[1]) : nullptr, nr, nt + 1, np),
+        rV3 = A(rV ? const_cast<double*>(rV[2]) : nullptr, nr, nt, np + 1);
 #pragma omp parallel for schedule(static)
     for (long k = 1; k <= np - 1; ++k)
         for (long j = 1; j <= nt - 1; ++j)
@@ -265,6 +274,7 @@ void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) {
                                 (((stt(i, j + 1, k + 1) + stt(i + 1, j + 1, k + 1)) * 0.5) + ((spp(i, j + 1, k + 1) + spp(i + 1, j + 1, k + 1)) * 0.5)) / aR +
                                 ((tRt(i, j, k) + tRt(i, j + 1, k)) * 0.5) / aR * cot(aT) -
                                 ((rG(i, j + 1, k + 1) + rG(i + 1, j + 1, k + 1)) * 0.5);
+                    if (rV) dV += rV1(i + 1, j + 1, k + 1);
                     VR(i + 1, j + 1, k + 1) = VR(i + 1, j + 1, k + 1) + dV * ((DT_R(i, j + 1, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
                 }
                 if (i <= nr - 2 && j <= nt + 1 - 2 && k <= np - 2) {
@@ -275,6 +285,7 @@ void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) {
                                 1.0 / aR / std::sin(aT) * (ttp(i, j, k + 1) - ttp(i, j, k)) * _dp +
                                 3.0 * ((tRt(i, j, k) + tRt(i + 1, j, k)) * 0.5) / aR +
                                 (((stt(i + 1, j, k + 1) + stt(i + 1, j + 1, k + 1)) * 0.5) - ((spp(i + 1, j, k + 1) + spp(i + 1, j + 1, k + 1)) * 0.5)) / aR * cot(aT);
+                    if (rV) dV += rV2(i + 1, j + 1, k + 1);
                     Vt(i + 1, j + 1, k + 1) = Vt(i + 1, j + 1, k + 1) + dV * ((DT_R(i + 1, j, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
                 }
                 if (i <= nr - 2 && j <= nt - 2 && k <= np + 1 - 2) {
@@ -285,10 +296,13 @@ void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) {
                                 1.0 / aR / std::sin(aT) * (spp(i + 1, j + 1, k + 1) - spp(i + 1, j + 1, k)) * _dp +
                                 3.0 * ((tRp(i, j, k) + tRp(i + 1, j, k)) * 0.5) / aR +
                                 2.0 * ((ttp(i, j, k) + ttp(i, j + 1, k)) * 0.5) / aR * cot(aT);
+                    if (rV) dV += rV3(i + 1, j + 1, k + 1);
                     Vp(i + 1, j + 1, k + 1) = Vp(i + 1, j + 1, k + 1) + dV * ((DT_R(i + 1, j + 1, k) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
                 }
             }
 }
+
+void orc_sph_compute_V(orc_sph_state* s, const orc_sph_params* q) { sph_compute_V_impl(s, q, nullptr); }
 
 // ---- boundary conditions ---------------------------------------------------
 // BC_R!  SphericalStokes_diapir.jl:61-69 (identical in SphericalStokes_plateau.jl:64-72)
@@ -678,6 +692,30 @@ int64_t orc_sph_residual_scratch_size(int64_t nr, int64_t nt, int64_t np) {
     int64_t nc = nr * nt * np;
     return nc + orc_sph_scratch_size(nr, nt, np) + 4 * nc + (nr - 1) * (nt - 1) * (np - 2) + (nr - 1) * (nt - 2) * (np - 1) +
            (nr - 2) * (nt - 1) * (np - 1);
+}
+
+// ---- EXT: correction sweeps of the mixed-precision solve ---------------------
+// One PT iteration of the correction problem per sweep: the state (P, V, τ) holds
+// the correction (δP, δV, δτ); η and ηSM are frozen (no maxloc!, no viscosity
+// update); rP is added to the divergence in the pressure update and rV (velocity
+// layouts) to the momentum rows in place of -ρg; the boundary conditions are the
+// homogeneous form of the BC set (diapir shear sh = 0, prescribed stresses 0).
+// The steps are those of the reference iteration (compute_P! :209-241, compute_V!
+// :308-329, BC_R!/BC_θ!/BC_φ! :61-99) with these right-hand sides.
+void orc_sph_corr_sweep(orc_sph_state* s, const orc_sph_params* q, const double* rP, const double* rVR, const double* rVt,
+                        const double* rVp, int64_t nsweeps) {
+    orc_sph_params h = *q;
+    h.sh = 0.0;
+    h.g = 0.0;
+    h.sig_t = 0.0;
+    h.sig_p = 0.0;
+    const double* rV[3] = {rVR, rVt, rVp};
+    for (int64_t it = 0; it < nsweeps; ++it) {
+        sph_compute_P_impl(s, &h, rP);
+        if (h.bc == 2) orc_sph_stress_pressure(s->P, s->ttt, s->tpp, s->nr, s->nt, s->np, 0.0, 0.0);
+        sph_compute_V_impl(s, &h, rV);
+        orc_sph_apply_bc(s, &h);
+    }
 }
 
 int32_t orc_num_threads(void) {

@@ -67,9 +67,21 @@ struct orc_cc_params {
     double dmp, vpdt, lr, g, tau_C, n_exp, relax, r, sh;
 };
 
+// right-hand sides of the correction problem of the mixed-precision solve (EXT): rP in the
+// pressure array's layout, rV1..rV3 in the velocity arrays' layouts
+struct orc_cc_rhs {
+    const double *rP, *rV1, *rV2, *rV3;
+};
+
 // ---------------------------------------------------------------------------
-// CylindricalStokes_diapir.jl: one PT iteration (:331-366), n_exp given
-void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
+// CylindricalStokes_diapir.jl: one PT iteration (:331-366), n_exp given.
+// rhs (EXT, may be NULL): a correction sweep instead — η and ηSM frozen (no
+// maxloc!, no power law), P -= KBDT (DIVV + rP), rV added to the momentum rows in
+// place of -ρg, the BCs in their homogeneous form (sh = 0).
+static void cyl_iterate_impl(orc_cc_state* s, const orc_cc_params* qin, int64_t niter, const orc_cc_rhs* rhs) {
+    orc_cc_params qh = *qin;
+    if (rhs) { qh.sh = 0.0; qh.g = 0.0; }
+    const orc_cc_params* q = &qh;
     const long nr = s->n1, nt = s->n2, nz = s->n3;
     const long nc = nr * nt * nz;
     std::vector<double> KBDT(nc), GSDT(nc), DIVV(nc), D_RR(nc), D_tt(nc), D_ZZ(nc), s_RR(nc), s_tt(nc), s_ZZ(nc), eta_pl_old(nc);
@@ -86,13 +98,17 @@ void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
     Arr DRt = A(D_Rt.data(), nr - 1, nt - 1, nz - 2), DRZ = A(D_RZ.data(), nr - 1, nt - 2, nz - 1), DtZ = A(D_tZ.data(), nr - 2, nt - 1, nz - 1);
     Arr dR = A(dVR.data(), nr - 1, nt - 2, nz - 2), dt_ = A(dVt.data(), nr - 2, nt - 1, nz - 2), dZ = A(dVZ.data(), nr - 2, nt - 2, nz - 1);
     Arr PLO = A(eta_pl_old.data(), nr, nt, nz);
+    Arr rV1 = A(rhs ? const_cast<double*>(rhs->rV1) : nullptr, nr + 1, nt, nz), rV2 = A(rhs ? const_cast<double*>(rhs->rV2) : nullptr, nr, nt + 1, nz),
+        rV3 = A(rhs ? const_cast<double*>(rhs->rV3) : nullptr, nr, nt, nz + 1);
     const double dr = q->d1, dth = q->d2, dz = q->d3, dmp = q->dmp, vpdt = q->vpdt, lr = q->lr;
     auto R = [&](long i, long, long) { return s->x1[i - 1]; };
     for (long it = 0; it < niter; ++it) {
         // equal!(ηSM, η); maxloc!; copy_bc_r/θ/z!(ηSM)                         :331-335
-        std::memcpy(s->etaSM, s->eta, sizeof(double) * nc);
-        maxloc_inn(s->etaSM, s->eta, nr, nt, nz);
-        copy_bc_full(s->etaSM, nr, nt, nz);
+        if (!rhs) {
+            std::memcpy(s->etaSM, s->eta, sizeof(double) * nc);
+            maxloc_inn(s->etaSM, s->eta, nr, nt, nz);
+            copy_bc_full(s->etaSM, nr, nt, nz);
+        }
         // timesteps!, timesteps2!                                                :336-337, :131-142
         for (long c = 0; c < nc; ++c) {
             KBDT[c] = dmp * 2.0 * PI * vpdt / lr * s->etaSM[c];
@@ -123,7 +139,8 @@ void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
                         DtZ(i, j, k) = 1 / avR * (VZ(i + 1, j + 1, k + 1) - VZ(i + 1, j, k + 1)) / dth + (Vt(i + 1, j + 1, k + 1) - Vt(i + 1, j + 1, k)) / dz;
                     }
                     if (i <= nr && j <= nt && k <= nz) {
-                        P(i, j, k) = P(i, j, k) - Kb(i, j, k) * Dv(i, j, k);
+                        const double dv = rhs ? Dv(i, j, k) + rhs->rP[(i - 1) + nr * ((j - 1) + nt * (k - 1))] : Dv(i, j, k);
+                        P(i, j, k) = P(i, j, k) - Kb(i, j, k) * dv;
                         tRR(i, j, k) = (tRR(i, j, k) + Gs(i, j, k) * 2.0 * DRR(i, j, k)) / (1.0 + Gs(i, j, k) / eta(i, j, k));
                         ttt(i, j, k) = (ttt(i, j, k) + Gs(i, j, k) * 2.0 * Dtt(i, j, k)) / (1.0 + Gs(i, j, k) / eta(i, j, k));
                         tZZ(i, j, k) = (tZZ(i, j, k) + Gs(i, j, k) * 2.0 * DZZ(i, j, k)) / (1.0 + Gs(i, j, k) / eta(i, j, k));
@@ -147,7 +164,7 @@ void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
         // compute_sigma!                                                         :170-176
         for (long c = 0; c < nc; ++c) { s_RR[c] = -s->P[c] + s->t11[c]; s_tt[c] = -s->P[c] + s->t22[c]; s_ZZ[c] = -s->P[c] + s->t33[c]; }
         // power law block (n_exp > 1)                                            :345-352
-        if (q->n_exp > 1) {
+        if (!rhs && q->n_exp > 1) {
             for (long k = 1; k <= nz - 2; ++k)
                 for (long j = 1; j <= nt - 2; ++j)
                     for (long i = 1; i <= nr - 2; ++i)
@@ -190,9 +207,21 @@ void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
         for (long k = 1; k <= nz - 1; ++k)
             for (long j = 1; j <= nt - 1; ++j)
                 for (long i = 1; i <= nr - 1; ++i) {
-                    if (j <= nt - 2 && k <= nz - 2) VR(i + 1, j + 1, k + 1) = VR(i + 1, j + 1, k + 1) + dR(i, j, k) * ((DT_R(i, j + 1, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
-                    if (i <= nr - 2 && k <= nz - 2) Vt(i + 1, j + 1, k + 1) = Vt(i + 1, j + 1, k + 1) + dt_(i, j, k) * ((DT_R(i + 1, j, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
-                    if (i <= nr - 2 && j <= nt - 2) VZ(i + 1, j + 1, k + 1) = VZ(i + 1, j + 1, k + 1) + dZ(i, j, k) * ((DT_R(i + 1, j + 1, k) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
+                    if (j <= nt - 2 && k <= nz - 2) {
+                        double r = dR(i, j, k);
+                        if (rhs) r += rV1(i + 1, j + 1, k + 1);
+                        VR(i + 1, j + 1, k + 1) = VR(i + 1, j + 1, k + 1) + r * ((DT_R(i, j + 1, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
+                    }
+                    if (i <= nr - 2 && k <= nz - 2) {
+                        double r = dt_(i, j, k);
+                        if (rhs) r += rV2(i + 1, j + 1, k + 1);
+                        Vt(i + 1, j + 1, k + 1) = Vt(i + 1, j + 1, k + 1) + r * ((DT_R(i + 1, j, k + 1) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
+                    }
+                    if (i <= nr - 2 && j <= nt - 2) {
+                        double r = dZ(i, j, k);
+                        if (rhs) r += rV3(i + 1, j + 1, k + 1);
+                        VZ(i + 1, j + 1, k + 1) = VZ(i + 1, j + 1, k + 1) + r * ((DT_R(i + 1, j + 1, k) + DT_R(i + 1, j + 1, k + 1)) * 0.5);
+                    }
                 }
         // boundary conditions                                                    :358-366
         const double r = q->r, sh = q->sh;
@@ -212,9 +241,14 @@ void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
     }
 }
 
+void orc_cyl_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) { cyl_iterate_impl(s, q, niter, nullptr); }
+
 // ---------------------------------------------------------------------------
-// CartesianStokes_diapir.jl: one PT iteration (:351-379)
-void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
+// CartesianStokes_diapir.jl: one PT iteration (:351-379); rhs as for the cylindrical script
+static void cart_iterate_impl(orc_cc_state* s, const orc_cc_params* qin, int64_t niter, const orc_cc_rhs* rhs) {
+    orc_cc_params qh = *qin;
+    if (rhs) { qh.sh = 0.0; qh.g = 0.0; }
+    const orc_cc_params* q = &qh;
     const long nx = s->n1, ny = s->n2, nz = s->n3;
     const long nc = nx * ny * nz;
     std::vector<double> eta_pl_old(nc);
@@ -223,10 +257,14 @@ void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
     Arr tXY = A(s->t12, nx - 1, ny - 1, nz - 2), tXZ = A(s->t13, nx - 1, ny - 2, nz - 1), tYZ = A(s->t23, nx - 2, ny - 1, nz - 1);
     Arr eta = A(s->eta, nx, ny, nz), etaSM = A(s->etaSM, nx, ny, nz), DT_R = A(s->DT_R, nx, ny, nz), tII = A(s->tII, nx, ny, nz), rho = A(s->rho, nx, ny, nz);
     const double _dx = 1.0 / q->d1, _dy = 1.0 / q->d2, _dz = 1.0 / q->d3, dmp = q->dmp, vpdt = q->vpdt, lx = q->lr, g = q->g;
+    Arr rV1 = A(rhs ? const_cast<double*>(rhs->rV1) : nullptr, nx + 1, ny, nz), rV2 = A(rhs ? const_cast<double*>(rhs->rV2) : nullptr, nx, ny + 1, nz),
+        rV3 = A(rhs ? const_cast<double*>(rhs->rV3) : nullptr, nx, ny, nz + 1);
     for (long it = 0; it < niter; ++it) {
-        std::memcpy(s->etaSM, s->eta, sizeof(double) * nc);                 // equal!(ηSM, η)
-        maxloc_inn(s->etaSM, s->eta, nx, ny, nz);                           // maxloc!
-        copy_boundary_faces(s->etaSM, nx, ny, nz);                          // copy_boundary!(ηSM)
+        if (!rhs) {
+            std::memcpy(s->etaSM, s->eta, sizeof(double) * nc);             // equal!(ηSM, η)
+            maxloc_inn(s->etaSM, s->eta, nx, ny, nz);                       // maxloc!
+            copy_boundary_faces(s->etaSM, nx, ny, nz);                      // copy_boundary!(ηSM)
+        }
         auto KB = [&](long i, long j, long k) { return dmp * 2.0 * PI * vpdt / lx * etaSM(i, j, k); };
         auto GS = [&](long i, long j, long k) { return 4.0 * PI * vpdt / lx * etaSM(i, j, k); };
         for (long k = 1; k <= nz; ++k)                                      // timesteps!  :132-138
@@ -236,7 +274,8 @@ void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
             for (long j = 1; j <= ny; ++j)
                 for (long i = 1; i <= nx; ++i) {
                     double Dxx = (VX(i + 1, j, k) - VX(i, j, k)) * _dx, Dyy = (VY(i, j + 1, k) - VY(i, j, k)) * _dy, Dzz = (VZ(i, j, k + 1) - VZ(i, j, k)) * _dz;
-                    P(i, j, k) = P(i, j, k) - KB(i, j, k) * (Dxx + Dyy + Dzz);
+                    const double dv = rhs ? (Dxx + Dyy + Dzz) + rhs->rP[(i - 1) + nx * ((j - 1) + ny * (k - 1))] : (Dxx + Dyy + Dzz);
+                    P(i, j, k) = P(i, j, k) - KB(i, j, k) * dv;
                     tXX(i, j, k) = (tXX(i, j, k) + GS(i, j, k) * 2.0 * Dxx) / (1.0 + GS(i, j, k) / eta(i, j, k));
                     tYY(i, j, k) = (tYY(i, j, k) + GS(i, j, k) * 2.0 * Dyy) / (1.0 + GS(i, j, k) / eta(i, j, k));
                     tZZ(i, j, k) = (tZZ(i, j, k) + GS(i, j, k) * 2.0 * Dzz) / (1.0 + GS(i, j, k) / eta(i, j, k));
@@ -262,7 +301,7 @@ void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
                         tYZ(i, j, k) = (tYZ(i, j, k) + aG * D) / (1.0 + aG / aE);
                     }
                 }
-        if (q->n_exp > 1) {                                                 // :358-363
+        if (!rhs && q->n_exp > 1) {                                         // :358-363
             for (long k = 1; k <= nz - 2; ++k)
                 for (long j = 1; j <= ny - 2; ++j)
                     for (long i = 1; i <= nx - 2; ++i)
@@ -284,17 +323,20 @@ void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
                     if (j <= ny - 2 && k <= nz - 2) {
                         double dV = -(P(i + 1, j + 1, k + 1) - P(i, j + 1, k + 1)) * _dx + (tXX(i + 1, j + 1, k + 1) - tXX(i, j + 1, k + 1)) * _dx +
                                     (tXY(i, j + 1, k) - tXY(i, j, k)) * _dy + (tXZ(i, j, k + 1) - tXZ(i, j, k)) * _dz;
+                        if (rhs) dV += rV1(i + 1, j + 1, k + 1);
                         VX(i + 1, j + 1, k + 1) = VX(i + 1, j + 1, k + 1) + dV * 0.5 * (DT_R(i, j + 1, k + 1) + DT_R(i + 1, j + 1, k + 1));
                     }
                     if (i <= nx - 2 && k <= nz - 2) {
                         double dV = (tXY(i + 1, j, k) - tXY(i, j, k)) * _dx - (P(i + 1, j + 1, k + 1) - P(i + 1, j, k + 1)) * _dy +
                                     (tYY(i + 1, j + 1, k + 1) - tYY(i + 1, j, k + 1)) * _dy + (tYZ(i, j, k + 1) - tYZ(i, j, k)) * _dz;
+                        if (rhs) dV += rV2(i + 1, j + 1, k + 1);
                         VY(i + 1, j + 1, k + 1) = VY(i + 1, j + 1, k + 1) + dV * 0.5 * (DT_R(i + 1, j, k + 1) + DT_R(i + 1, j + 1, k + 1));
                     }
                     if (i <= nx - 2 && j <= ny - 2) {
                         double dV = (tXZ(i + 1, j, k) - tXZ(i, j, k)) * _dx + (tYZ(i, j + 1, k) - tYZ(i, j, k)) * _dy -
                                     (P(i + 1, j + 1, k + 1) - P(i + 1, j + 1, k)) * _dz + (tZZ(i + 1, j + 1, k + 1) - tZZ(i + 1, j + 1, k)) * _dz -
                                     g * (0.5 * (rho(i + 1, j + 1, k) + rho(i + 1, j + 1, k + 1)));
+                        if (rhs) dV += rV3(i + 1, j + 1, k + 1);
                         VZ(i + 1, j + 1, k + 1) = VZ(i + 1, j + 1, k + 1) + dV * 0.5 * (DT_R(i + 1, j + 1, k) + DT_R(i + 1, j + 1, k + 1));
                     }
                 }
@@ -313,6 +355,17 @@ void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) {
         for (long j = 1; j <= ny + 1; ++j) for (long i = 1; i <= nx; ++i) { VY(i, j, 1) = VY(i, j, 2); VY(i, j, nz) = VY(i, j, nz - 1); }     // copy_bc_z!(VY)
         for (long j = 1; j <= ny; ++j) for (long i = 1; i <= nx; ++i) { VZ(i, j, 1) = -VZ(i, j, 2); VZ(i, j, nz + 1) = -VZ(i, j, nz); }       // bc_z_0!(VZ)
     }
+}
+
+void orc_cart_iterate(orc_cc_state* s, const orc_cc_params* q, int64_t niter) { cart_iterate_impl(s, q, niter, nullptr); }
+
+// EXT: nsweeps correction sweeps of the mixed-precision solve (geometry 1 cylindrical, 2 Cartesian);
+// s holds the correction state, η and ηSM frozen
+void orc_cc_corr_sweep(int32_t geometry, orc_cc_state* s, const orc_cc_params* q, const double* rP, const double* rV1,
+                       const double* rV2, const double* rV3, int64_t nsweeps) {
+    const orc_cc_rhs rhs{rP, rV1, rV2, rV3};
+    if (geometry == 1) cyl_iterate_impl(s, q, nsweeps, &rhs);
+    else cart_iterate_impl(s, q, nsweeps, &rhs);
 }
 
 }  // extern "C"

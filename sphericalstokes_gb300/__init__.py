@@ -46,6 +46,13 @@ ALIASES = {
     "η": "ETA", "η_ini": "ETA_INI", "ηSM": "ETA_SM", "τII": "TII", "ρ": "RHO",
 }
 KERNELS = {"maxloc": 0, "compute_P": 1, "rheology": 2, "compute_V": 3, "bc": 4}
+# fields of the correction problem of the mixed-precision solve (sph_corr_field) and the
+# reference-layout field whose size each one has
+CORR_FIELDS = {
+    "dP": (0, "P"), "dV1": (1, "V1"), "dV2": (2, "V2"), "dV3": (3, "V3"), "dTAU11": (4, "TAU11"), "dTAU22": (5, "TAU22"),
+    "dTAU33": (6, "TAU33"), "dTAU12": (7, "TAU12"), "dTAU13": (8, "TAU13"), "dTAU23": (9, "TAU23"), "ETA": (10, "P"),
+    "ETA_SM": (11, "P"), "rP": (12, "P"), "rV1": (13, "V1"), "rV2": (14, "V2"), "rV3": (15, "V3"),
+}
 
 
 class SphError(RuntimeError):
@@ -124,6 +131,10 @@ _SIGS = {
                   C.c_int64], C.c_int),
     "sph_check_err_noalloc": ([C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_int64),
                                C.POINTER(C.c_double), C.c_void_p], C.c_int),
+    "sph_corr_get": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
+    "sph_corr_set": ([C.c_void_p, C.c_int32, C.POINTER(C.c_double), C.c_int64], C.c_int),
+    "sph_selftest_wait_timeout": ([C.c_void_p], C.c_int),
+    "sph_solve_history_ms": ([C.c_void_p, C.POINTER(C.c_double), C.c_int64, C.POINTER(C.c_int64)], C.c_int),
 }
 
 _lib = None
@@ -311,6 +322,15 @@ class Solver:
                            float(info.seconds), hi[:n].copy(), he[:n].copy(), float(info.device_ms), float(info.sweep_ms),
                            float(info.outer_ms))
 
+    def history_ms(self) -> np.ndarray:
+        """Wall-clock ms from the start of the last solve to each of its history entries."""
+        n = C.c_int64()
+        _check(self.lib, self.lib.sph_solve_history_ms(self._h, None, 0, C.byref(n)), "sph_solve_history_ms")
+        out = np.zeros(int(n.value), dtype=np.float64)
+        _check(self.lib, self.lib.sph_solve_history_ms(self._h, out.ctypes.data_as(C.POINTER(C.c_double)), len(out),
+                                                       C.byref(n)), "sph_solve_history_ms")
+        return out
+
     def autotune(self, sweeps: int = 20) -> tuple[int, float]:
         """Pick the fused sweep's x3 chunk length for this grid size; returns (chunk, ms per sweep)."""
         k, ms = C.c_int32(), C.c_double()
@@ -346,6 +366,23 @@ class Solver:
 
     def sweep_apply(self) -> None:
         _check(self.lib, self.lib.sph_sweep_apply(self._h), "sph_sweep_apply")
+
+    def corr_get(self, name: str) -> np.ndarray:
+        """A field of the correction problem sph_sweep iterates (``CORR_FIELDS``), reference layout."""
+        fid, like = CORR_FIELDS[name]
+        out = np.zeros(self.dims(like), dtype=np.float64, order="F")
+        _check(self.lib, self.lib.sph_corr_get(self._h, fid, out.ctypes.data_as(C.POINTER(C.c_double)), out.size),
+               f"corr_get {name}")
+        return out
+
+    def corr_set(self, name: str, a) -> None:
+        """Overwrite a field of the correction problem (stored as FP32)."""
+        fid, like = CORR_FIELDS[name]
+        a = np.asfortranarray(np.asarray(a, dtype=np.float64))
+        if a.shape != self.dims(like):
+            raise ValueError(f"{name}: expected shape {self.dims(like)}, got {a.shape}")
+        _check(self.lib, self.lib.sph_corr_set(self._h, fid, a.ctypes.data_as(C.POINTER(C.c_double)), a.size),
+               f"corr_set {name}")
 
     def residual(self) -> dict:
         out = (C.c_double * 7)()

@@ -93,8 +93,16 @@ __device__ __forceinline__ bool traction_pressure(int j, int k, int n2, int n3, 
     return true;
 }
 
-// order-preserving bits of a non-negative double (NaN maps above +inf)
-__device__ __forceinline__ unsigned long long ord_bits(double x) { return (unsigned long long)__double_as_longlong(x); }
+// Order-preserving bits of |x|: for non-negative doubles the unsigned order of the
+// bit patterns is the numeric order, and every NaN is mapped to the canonical
+// positive quiet NaN 0x7ff8000000000000, which lies above +inf.  A max taken on
+// these bits (shuffles, atomicMax) therefore propagates NaN, as Julia's maximum
+// does, instead of dropping it (fmax) or folding it into +inf.
+__device__ __forceinline__ unsigned long long ord_bits(double x) {
+    x = fabs(x);
+    return x != x ? 0x7ff8000000000000ULL : (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ unsigned long long umax64(unsigned long long a, unsigned long long b) { return a > b ? a : b; }
 
 // max with NaN propagation (Julia's `max`)
 template <typename T>

@@ -302,21 +302,37 @@ __device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 // bounded wait on the phase with the given parity; false if the bound ran out.
-// Each try_wait suspends the thread until the phase completes or kMbarSuspendNs
-// pass, so a waiting warp does not re-issue polls; kMbarMaxPolls of them bound
-// the wait to about 2 s.
+// Each try_wait suspends the thread until the phase completes or the suspend hint
+// (kMbarSuspendNs) passes, so a waiting warp does not re-issue polls; kMbarMaxPolls
+// of them bound the wait to about 2 s.  The bound is a count of polls, so the wait
+// ends whatever the hint does.
 constexpr unsigned kMbarSuspendNs = 200000;
 constexpr int kMbarMaxPolls = 10000;
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int max_polls = kMbarMaxPolls,
+                                          unsigned suspend_ns = kMbarSuspendNs) {
     const unsigned a = smem_u32(bar);
-    for (int it = 0; it < kMbarMaxPolls; ++it) {
+    for (int it = 0; it < max_polls; ++it) {
         unsigned done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
-            : "=r"(done) : "r"(a), "r"(parity), "r"(kMbarSuspendNs) : "memory");
+            : "=r"(done) : "r"(a), "r"(parity), "r"(suspend_ns) : "memory");
         if (done) return true;
     }
     return false;
+}
+
+// Self-test of the bounded-wait error path of the TMA sweeps: one block waits on an
+// mbarrier that nothing completes (initialised for one arrival, never arrived at, no
+// copy issued), with the sweeps' wait at max_polls polls of suspend_ns; when the
+// bound runs out it records 1 in *err as the sweep kernels do, and returns.
+__global__ void k_wait_selftest(int* err, int max_polls, unsigned suspend_ns) {
+    __shared__ unsigned long long bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && !mbar_wait(&bar, 0u, max_polls, suspend_ns)) atomicExch(err, 1);
 }
 __device__ __forceinline__ void tma_load3d(float* dst, const CUtensorMap* map, int x, int y, int z, unsigned long long* bar) {
     asm volatile(
@@ -422,7 +438,7 @@ __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4,
 // the block barrier that follows passes the completed copies on to the other
 // warps, so nine of ten warps never poll.  A chunk copies only the planes it
 // uses (inputs kA-1 .. kB, old state and rV kA-1 .. kB-1), so nothing is in
-// flight when the march ends.
+// flight when the march ends (unless a bounded wait ran out, see the end).
 //
 // Per-plane work is kept free of per-thread branching, which this kernel pays
 // for in issue slots (it is instruction-bound): every stage-1 thread evaluates
@@ -481,15 +497,19 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             for (int f = 0; f < F_RV; ++f) tma_load3d(S.rv[sl][f], maps + TM_RV1 + f, x0, y0, z, &S.bar_old[sl]);
     };
     unsigned ph_in = 0, ph_old = 0;  // parity bit per ring slot
+    // false once a bounded wait ran out: from then on this thread neither waits nor (thread 0)
+    // issues copies, so the block finishes its march on whatever the tiles hold and exits
     bool ok = true;
     auto wait_in = [&](int z) {
+        if (!ok) return;
         const int sl = (z + 3) % 3;
-        ok &= mbar_wait(&S.bar_in[sl], (ph_in >> sl) & 1u);
+        ok = mbar_wait(&S.bar_in[sl], (ph_in >> sl) & 1u);
         ph_in ^= 1u << sl;
     };
     auto wait_old = [&](int z) {
+        if (!ok) return;
         const int sl = z & 1;
-        ok &= mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
+        ok = mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
         ph_old ^= 1u << sl;
     };
 
@@ -658,7 +678,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             wait_old(K);
         }
         __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
-        if (tid == 0) {  // only planes the chunk uses: inputs up to kB, old state and rV up to kB - 1
+        if (tid == 0 && ok) {  // only planes the chunk uses: inputs up to kB, old state and rV up to kB - 1
             if (K + 2 <= kB) issue_inputs(K + 2);
             if (K + 1 <= kB - 1) issue_old(K + 1);
         }
@@ -672,7 +692,11 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         if (K <= n3 - 3) step(K, std::true_type{});
         else step(K, std::false_type{});
     }
-    if (waiter && !ok && err) atomicExch(err, 1);  // every issued copy has been waited for: none is in flight
+    // Without a time-out every issued copy has been waited for, so none is in flight when the
+    // block exits.  After a time-out copies issued before it may still be landing in this
+    // block's shared memory as it exits and the state it wrote is suspect: the host reads the
+    // flag after the launch and treats it as fatal for the context.
+    if (waiter && !ok && err) atomicExch(err, 1);
 }
 
 inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }

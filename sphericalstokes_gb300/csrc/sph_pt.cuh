@@ -286,28 +286,25 @@ template <typename T, int G>
 __global__ void __launch_bounds__(256) k_velocity_norm(KP<T> p) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1, K = blockIdx.z + 1;
     const Dims& d = p.d;
-    double m = 0.0;
+    unsigned long long m = 0ULL;  // ordered bits of the running max (NaN propagates)
     if (I <= d.n1 - 1 && J <= d.n2 - 1 && K <= d.n3 - 1) {
         T dv[3];
         bool ok[3];
         momentum<T, G, false, true>(p, I, J, K, dv, ok);
         for (int f = 0; f < 3; ++f)
-            if (ok[f]) {
-                double x = fabs((double)dv[f]);
-                m = fmax(m, x != x ? (double)INFINITY : x);
-            }
+            if (ok[f]) m = umax64(m, ord_bits((double)dv[f]));
     }
     // block reduction over the 2D block
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    __shared__ double sm[32];
+    for (int o = 16; o > 0; o >>= 1) m = umax64(m, __shfl_xor_sync(0xffffffffu, m, o));
+    __shared__ unsigned long long sm[32];
     const int t = threadIdx.x + blockDim.x * threadIdx.y;
     const int lane = t & 31, w = t >> 5, nw = (blockDim.x * blockDim.y) >> 5;
     if (lane == 0) sm[w] = m;
     __syncthreads();
     if (w == 0) {
-        m = lane < nw ? sm[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) atomicMax(p.red, ord_bits(m));
+        m = lane < nw ? sm[lane] : 0ULL;
+        for (int o = 16; o > 0; o >>= 1) m = umax64(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) atomicMax(p.red, m);
     }
 }
 
@@ -449,30 +446,27 @@ __global__ void k_traction_pressure(KP<T> p, T* __restrict__ Pout) {
 }
 
 // ---------------------------------------------------------------------------
-// reductions: max|a| (or max|a-b|) over n entries into red[slot]
-// block-wide max of non-negative values (NaN mapped to +inf by the caller),
-// one atomicMax per block on the order-preserving bits
-__device__ __forceinline__ void block_max_to(double v, unsigned long long* slot) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    __shared__ double sm[32];
+// reductions: max|a| (or max|a-b|) over n entries into red[slot], as the ordered
+// bits of ord_bits (a NaN entry makes the result NaN, as Julia's maximum(abs.(.)))
+// block-wide max of ordered bits, one atomicMax per block
+__device__ __forceinline__ void block_max_to(unsigned long long v, unsigned long long* slot) {
+    for (int o = 16; o > 0; o >>= 1) v = umax64(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ unsigned long long sm[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     if (lane == 0) sm[w] = v;
     __syncthreads();
     if (w == 0) {
-        v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (lane == 0) atomicMax(slot, ord_bits(v));
+        v = lane < (int)(blockDim.x >> 5) ? sm[lane] : 0ULL;
+        for (int o = 16; o > 0; o >>= 1) v = umax64(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) atomicMax(slot, v);
     }
 }
 
 template <typename T>
 __global__ void k_maxabs(const T* __restrict__ a, const T* __restrict__ b, long long n, unsigned long long* slot) {
-    double m = 0.0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
-        double x = b ? (double)a[q] - (double)b[q] : (double)a[q];
-        x = fabs(x);
-        m = fmax(m, (x != x) ? (double)INFINITY : x);
-    }
+    unsigned long long m = 0ULL;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+        m = umax64(m, ord_bits(b ? (double)a[q] - (double)b[q] : (double)a[q]));
     block_max_to(m, slot);
 }
 
@@ -486,6 +480,31 @@ __global__ void k_convert(TD* __restrict__ dst, const TS* __restrict__ src, long
 template <typename TS>
 __global__ void k_add_widen(double* __restrict__ dst, const TS* __restrict__ src, long long n) {
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) dst[q] += (double)src[q];
+}
+
+// A field in the reference layout (dense e0 x e1 x e2 doubles, x1 fastest) <-> its
+// entries in the padded box (strides 1, sy, sz).  Launch: grid (ceil(e0/blockDim.x),
+// e1, e2); one entry per thread, consecutive threads on consecutive x1 entries on
+// both sides.  The host copies whole dense fields in one transfer and these kernels
+// do the re-pitching on the device.
+template <typename T>
+__device__ __forceinline__ T from_double(double v) { return (T)v; }
+template <>
+__device__ __forceinline__ uint8_t from_double<uint8_t>(double v) { return v != 0.0 ? 1 : 0; }
+
+template <typename T>
+__global__ void k_unpack(T* __restrict__ box, const double* __restrict__ dense, int e0, int e1, int sy, int sz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e0) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    box[i + (long long)sy * j + (long long)sz * k] = from_double<T>(dense[i + (long long)e0 * (j + (long long)e1 * k)]);
+}
+template <typename T>
+__global__ void k_pack(double* __restrict__ dense, const T* __restrict__ box, int e0, int e1, int sy, int sz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= e0) return;
+    const int j = blockIdx.y, k = blockIdx.z;
+    dense[i + (long long)e0 * (j + (long long)e1 * k)] = (double)box[i + (long long)sy * j + (long long)sz * k];
 }
 
 }  // namespace sph

@@ -125,15 +125,18 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
         for (int f = 0; f < F_RV; ++f) tma_load3d(S.rv[sl][f], maps + TM_RV1 + f, x0, y0, z, &S.bar_old[sl]);
     };
     unsigned ph_in = 0, ph_old = 0;  // parity bit per ring slot
+    // false once a bounded wait ran out: no further waits or copies (as in k_fused_tma)
     bool ok = true;
     auto wait_in = [&](int z) {
+        if (!ok) return;
         const int sl = (z + 3) % 3;
-        ok &= mbar_wait(&S.bar_in[sl], (ph_in >> sl) & 1u);
+        ok = mbar_wait(&S.bar_in[sl], (ph_in >> sl) & 1u);
         ph_in ^= 1u << sl;
     };
     auto wait_old = [&](int z) {
+        if (!ok) return;
         const int sl = z & 1;
-        ok &= mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
+        ok = mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
         ph_old ^= 1u << sl;
     };
 
@@ -328,7 +331,7 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
             wait_old(K);
         }
         __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
-        if (tid == 0) {
+        if (tid == 0 && ok) {
             issue_inputs(K + 2);
             issue_old(K + 1);
         }
@@ -336,7 +339,8 @@ __global__ void __launch_bounds__(X2_NT, 3) k_sweep_x2(KP<float> p, FusedOut<flo
         __syncthreads();
         velocity(K);
     }
-    // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits
+    // drain the copies still in flight (planes kB+1 inputs, kB old) before the block exits;
+    // after a time-out some may still be landing (the host treats the flag as fatal)
     if (waiter) {
         wait_in(kB + 1);
         wait_old(kB);

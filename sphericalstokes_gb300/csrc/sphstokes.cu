@@ -128,6 +128,11 @@ struct Ctx {
     std::vector<cudaEvent_t> prof_ev;
     size_t prof_next = 0;
     bool prof_on = false;
+    double* stage = nullptr;  // dense staging field of the host copies (vol doubles), allocated on first use
+    // wall-clock ms from the start of the last sph_solve to each of its history entries
+    std::vector<double> hist_ms;
+    std::chrono::steady_clock::time_point solve_t0;
+    bool broken = false;      // a bounded wait of a sweep kernel ran out: the context's state is suspect
 };
 
 constexpr int kRedSlots = 16;
@@ -740,6 +745,46 @@ int compute_f_scale(Ctx& c) {
 }
 
 // ---------------------------------------------------------------------------
+// host <-> device copies of one field: one contiguous transfer of the dense field
+// (the reference layout, e0 x e1 x e2 doubles) to or from a staging buffer, and a
+// re-pitching kernel between the staging buffer and the padded box, so the copy engine
+// moves a single large block instead of e1*e2 short rows
+int ensure_stage(Ctx& c) {
+    if (c.stage) return SPH_OK;
+    if (cudaMalloc((void**)&c.stage, sizeof(double) * c.d.vol) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SPH_ERR_NOMEM, "staging buffer of the host copies");
+    }
+    return SPH_OK;
+}
+inline dim3 pack_grid(const int e[3]) { return dim3((e[0] + 127) / 128, e[1], e[2]); }
+
+// host (dense doubles) -> box (converted to T); returns after the host buffer has been read
+template <typename T>
+int upload_box(Ctx& c, T* box, const int e[3], const double* host) {
+    int rc = ensure_stage(c);
+    if (rc) return rc;
+    const size_t n = (size_t)e[0] * e[1] * e[2];
+    CK(cudaMemcpyAsync(c.stage, host, sizeof(double) * n, cudaMemcpyHostToDevice, c.stream));
+    k_unpack<T><<<pack_grid(e), 128, 0, c.stream>>>(box, c.stage, e[0], e[1], c.d.sy, c.d.sz);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(c.stream));
+    return SPH_OK;
+}
+// box (T) -> host (dense doubles); returns after the host buffer is written
+template <typename T>
+int download_box(Ctx& c, const T* box, const int e[3], double* host) {
+    int rc = ensure_stage(c);
+    if (rc) return rc;
+    const size_t n = (size_t)e[0] * e[1] * e[2];
+    k_pack<T><<<pack_grid(e), 128, 0, c.stream>>>(c.stage, box, e[0], e[1], c.d.sy, c.d.sz);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(host, c.stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+    CK(cudaStreamSynchronize(c.stream));
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
 // plain PT solve (FP64 or FP32 state)
 template <typename T>
 int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_solve_info* info, int64_t* hi, double* he, int64_t cap) {
@@ -772,6 +817,7 @@ int solve_plain(Ctx& c, State<T>& s, bool is32, const sph_solve_opts& o, sph_sol
             if (hi) hi[info->nhist] = it;
             if (he) he[info->nhist] = err;
             info->nhist++;
+            c.hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c.solve_t0).count());
         }
         if (!(err == err) || std::isinf(err)) { status = SPH_ERR_DIVERGED; break; }
         if (c.prm.switch_err > 0.0 && err < c.prm.switch_err) c.cur_n = c.prm.n_exp_late;
@@ -859,6 +905,8 @@ const CUtensorMap* tma_maps(Ctx& c) {
         if (c.map_key[i] == t.f[F_V1]) return c.d_maps + i * TM_COUNT;
     if (!c.d_maps) {
         if (cudaMalloc((void**)&c.d_maps, sizeof(CUtensorMap) * 2 * TM_COUNT) != cudaSuccess) { c.use_tma = false; return nullptr; }
+    }
+    if (!c.d_err) {
         if (cudaMalloc((void**)&c.d_err, sizeof(int)) != cudaSuccess) { c.use_tma = false; return nullptr; }
         cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream);
     }
@@ -891,15 +939,27 @@ void ensure_tma_maps(Ctx& c) {
     swap_state(c.s32);
 }
 
+// The error word of the TMA sweep kernels: set when a bounded wait on a copy barrier ran
+// out.  The kernel then stopped issuing copies and finished its march on whatever its
+// tiles held, so the FP32 state is suspect and copies may have been in flight when its
+// blocks exited: the context is marked unusable (every later call that would launch work
+// on it fails) and the caller destroys it.
 int check_kernel_flag(Ctx& c) {
     if (!c.d_err) return SPH_OK;
     int h = 0;
     CK(cudaMemcpyAsync(&h, c.d_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     CK(cudaStreamSynchronize(c.stream));
     if (h) {
-        CK(cudaMemsetAsync(c.d_err, 0, sizeof(int), c.stream));
-        return fail(SPH_ERR_CUDA, "a bounded wait on a TMA barrier ran out in the fused sweep");
+        c.broken = true;
+        return fail(SPH_ERR_CUDA, "a bounded wait on a TMA barrier ran out in the fused sweep; the context is unusable");
     }
+    return SPH_OK;
+}
+
+// SPH_OK, or the failure every entry point that launches work returns on a context
+// marked unusable by check_kernel_flag
+int usable(const Ctx& c) {
+    if (c.broken) return fail(SPH_ERR_CUDA, "context unusable: a bounded wait of a sweep kernel ran out earlier; destroy it");
     return SPH_OK;
 }
 
@@ -1008,6 +1068,18 @@ int apply_correction(Ctx& c) {
     CK(cudaGetLastError());
     c.corr_ready = false;
     return SPH_OK;
+}
+
+// the correction problem of the current FP64 state, prepared unless one is (MIXED)
+int ensure_correction(Ctx& c) {
+    if (c.corr_ready) return SPH_OK;
+    int rc = sync64(c);
+    if (rc) return rc;
+    double out[7];
+    const int G = c.prm.geometry;
+    rc = G == SPH ? outer_residual<SPH>(c, out) : (G == CYL ? outer_residual<CYL>(c, out) : outer_residual<CART>(c, out));
+    if (rc) return rc;
+    return G == SPH ? prepare_correction<SPH>(c, out) : (G == CYL ? prepare_correction<CYL>(c, out) : prepare_correction<CART>(c, out));
 }
 
 // the captured launches of a context (correction sweeps, warm-start iterations): dropped
@@ -1119,6 +1191,7 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
                 if (hi) hi[info->nhist] = iters;
                 if (he) he[info->nhist] = err;
                 info->nhist++;
+                c.hist_ms.push_back(std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - c.solve_t0).count());
             }
             info->outer = outer;
             info->residual = err;
@@ -1182,6 +1255,8 @@ int check_params(const sph_params* p) {
     if (p->rheology < 0 || p->rheology > 3) return fail(SPH_ERR_INVALID, "rheology");
     if (p->bc < 0 || p->bc > 2) return fail(SPH_ERR_INVALID, "bc");
     if (p->n1 < 5 || p->n2 < 5 || p->n3 < 5) return fail(SPH_ERR_INVALID, "grid needs at least 5 cells per axis");
+    // x2 and x3 index the launch grids' y and z dimensions (at most 65535 blocks each)
+    if (p->n2 >= 65535 || p->n3 >= 65535) return fail(SPH_ERR_INVALID, "n2 and n3 must be below 65535");
     if (!(p->l1 > 0 && p->l2 > 0 && p->l3 > 0 && p->l_ref > 0)) return fail(SPH_ERR_INVALID, "lengths must be positive");
     long long px = ((p->n1 + 1 + 31) / 32) * 32LL;
     if (px * (p->n2 + 1LL) * (p->n3 + 1LL) >= (1LL << 31)) return fail(SPH_ERR_INVALID, "grid too large for 32-bit indexing");
@@ -1364,6 +1439,7 @@ int sph_batch_solve(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sp
 int sph_autotune(void* h, int32_t sweeps, int32_t* best_chunk, double* best_ms) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (c->prm.precision != SPH_PREC_MIXED || !c->fused) return fail(SPH_ERR_UNSUPPORTED, "sph_autotune tunes the fused FP32 sweep (MIXED, SPH_KERNELS_AUTO)");
     if (sweeps < 2) sweeps = 2;
     int rc = sph_sweep(h, 0);  // prepares a correction problem (FP64 state unchanged)
@@ -1409,6 +1485,7 @@ int sph_autotune(void* h, int32_t sweeps, int32_t* best_chunk, double* best_ms) 
 int sph_update_params(void* h, const sph_params* p) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     int rc = check_params(p);
     if (rc) return rc;
     const sph_params& q = c->prm;
@@ -1448,6 +1525,7 @@ int sph_destroy(void* h) {
     if (c->ev4) cudaEventDestroy(c->ev4);
     for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
     if (c->adj) cudaFree(c->adj);
+    if (c->stage) cudaFree(c->stage);
     if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return SPH_OK;
@@ -1469,45 +1547,23 @@ static int copy_field(Ctx* c, int32_t field, double* host, const double* src_hos
     if (count != need) return fail(SPH_ERR_INVALID, "count does not match the field size");
     if (!host && !src_host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
     const bool get = host != nullptr;
-    if (get) { int rc = sync64(*c); if (rc) return rc; }
-    if (field == SPH_FIELD_PHASE) {
-        std::vector<uint8_t> b((size_t)c->d.vol, 0);
-        if (get) { CK(cudaMemcpyAsync(b.data(), c->phase, c->d.vol, cudaMemcpyDeviceToHost, c->stream)); CK(cudaStreamSynchronize(c->stream)); }
-        for (int k = 0; k < e[2]; ++k)
-            for (int j = 0; j < e[1]; ++j)
-                for (int i = 0; i < e[0]; ++i) {
-                    long long bi = i + (long long)c->d.sy * j + (long long)c->d.sz * k;
-                    long long hi = i + (long long)e[0] * (j + (long long)e[1] * k);
-                    if (get) host[hi] = b[bi]; else b[bi] = src_host[hi] != 0.0 ? 1 : 0;
-                }
-        if (!get) { CK(cudaMemcpyAsync(c->phase, b.data(), c->d.vol, cudaMemcpyHostToDevice, c->stream)); CK(cudaStreamSynchronize(c->stream)); c->stale32 = true; }
-        return SPH_OK;
+    int rc = usable(*c);
+    if (rc) return rc;
+    if (get && (rc = sync64(*c))) return rc;
+    if (field == SPH_FIELD_PHASE) {  // stored as one byte per entry (1 = linear cell)
+        rc = get ? download_box<uint8_t>(*c, c->phase, e, host) : upload_box<uint8_t>(*c, c->phase, e, src_host);
+    } else {
+        double* dev = c->s64.f[slot_of(field)];
+        rc = get ? download_box<double>(*c, dev, e, host) : upload_box<double>(*c, dev, e, src_host);
     }
-    double* dev = c->s64.f[slot_of(field)];
-    cudaMemcpy3DParms m;
-    std::memset(&m, 0, sizeof(m));
-    cudaPitchedPtr dp = make_cudaPitchedPtr(dev, sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
-    cudaPitchedPtr hp = make_cudaPitchedPtr(get ? (void*)host : (void*)src_host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
-    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
-    if (get) { m.srcPtr = dp; m.dstPtr = hp; m.kind = cudaMemcpyDeviceToHost; }
-    else { m.srcPtr = hp; m.dstPtr = dp; m.kind = cudaMemcpyHostToDevice; }
-    CK(cudaMemcpy3DAsync(&m, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
+    if (rc) return rc;
     if (!get) c->stale32 = true;
     return SPH_OK;
 }
 
 // one FP64 state slot with the extent e, in the reference's column-major layout
 static int copy_slot_out(Ctx* c, int slot, const int e[3], double* host) {
-    cudaMemcpy3DParms m;
-    std::memset(&m, 0, sizeof(m));
-    m.srcPtr = make_cudaPitchedPtr(c->s64.f[slot], sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
-    m.dstPtr = make_cudaPitchedPtr(host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
-    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
-    m.kind = cudaMemcpyDeviceToHost;
-    CK(cudaMemcpy3DAsync(&m, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    return SPH_OK;
+    return download_box<double>(*c, c->s64.f[slot], e, host);
 }
 
 static std::string strf(const char* f, ...) {
@@ -1554,28 +1610,13 @@ static int adj_upload(Ctx* c, int slot, int field, const double* host) {
     if (!host) return SPH_OK;
     int e[3];
     field_extent(c->d, field, e);
-    cudaMemcpy3DParms m;
-    std::memset(&m, 0, sizeof(m));
-    m.srcPtr = make_cudaPitchedPtr(const_cast<double*>(host), sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
-    m.dstPtr = make_cudaPitchedPtr(dev, sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
-    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
-    m.kind = cudaMemcpyHostToDevice;
-    CK(cudaMemcpy3DAsync(&m, c->stream));
-    return SPH_OK;
+    return upload_box<double>(*c, dev, e, host);
 }
 static int adj_download(Ctx* c, int slot, int field, double* host) {
     if (!host) return SPH_OK;
     int e[3];
     field_extent(c->d, field, e);
-    cudaMemcpy3DParms m;
-    std::memset(&m, 0, sizeof(m));
-    m.srcPtr = make_cudaPitchedPtr(adj_slot(c, slot), sizeof(double) * c->d.px, sizeof(double) * c->d.px, c->d.py);
-    m.dstPtr = make_cudaPitchedPtr(host, sizeof(double) * e[0], sizeof(double) * e[0], e[1]);
-    m.extent = make_cudaExtent(sizeof(double) * e[0], e[1], e[2]);
-    m.kind = cudaMemcpyDeviceToHost;
-    CK(cudaMemcpy3DAsync(&m, c->stream));
-    CK(cudaStreamSynchronize(c->stream));
-    return SPH_OK;
+    return download_box<double>(*c, adj_slot(c, slot), e, host);
 }
 
 // KP of the adjoint: the FP64 state with η = the residual's viscosity (the law's target for
@@ -1706,6 +1747,7 @@ extern "C" {
 int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
     int rc = sync64(*c);
     if (rc) return rc;
@@ -1718,6 +1760,7 @@ int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
 int sph_get_field(void* h, int32_t field, double* host, int64_t count) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
     return copy_field(c, field, host, nullptr, count);
 }
@@ -1725,6 +1768,7 @@ int sph_get_field(void* h, int32_t field, double* host, int64_t count) {
 int sph_step(void* h, int64_t k) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
     const bool use32 = c->prm.precision != SPH_PREC_FP64;
     int rc = use32 ? sync32(*c) : sync64(*c);
@@ -1747,6 +1791,7 @@ int sph_step(void* h, int64_t k) {
 int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* hist_iter, double* hist_err, int64_t hist_cap) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !o) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (o->tol <= 0.0 || o->maxiter <= 0) return fail(SPH_ERR_INVALID, "tol and maxiter must be positive");
     if (o->criterion < SPH_CRIT_REFERENCE || o->criterion > SPH_CRIT_REFERENCE_PLATEAU) return fail(SPH_ERR_INVALID, "criterion");
     sph_solve_info local;
@@ -1754,6 +1799,8 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
     sph_solve_info* inf = info ? info : &local;
     std::memset(inf, 0, sizeof(*inf));
     auto t0 = std::chrono::steady_clock::now();
+    c->solve_t0 = t0;
+    c->hist_ms.clear();
     c->sweep_ms = c->outer_ms = 0.0;
     CK(cudaEventRecord(c->ev0, c->stream));
     int rc;
@@ -1800,21 +1847,14 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
 int sph_sweep(void* h, int64_t k) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (c->prm.precision != SPH_PREC_MIXED) return fail(SPH_ERR_UNSUPPORTED, "sph_sweep needs SPH_PREC_MIXED");
     if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
     if (c->prm.rheology == SPH_RHEO_TAU_POWER || c->prm.rheology == SPH_RHEO_TAU_POWER_RELAX)
         return fail(SPH_ERR_UNSUPPORTED, "mixed precision needs an explicit viscosity law (linear or strain-rate power law)");
     const int G = c->prm.geometry;
-    int rc;
-    if (!c->corr_ready) {
-        rc = sync64(*c);
-        if (rc) return rc;
-        double out[7];
-        rc = G == SPH ? outer_residual<SPH>(*c, out) : (G == CYL ? outer_residual<CYL>(*c, out) : outer_residual<CART>(*c, out));
-        if (rc) return rc;
-        rc = G == SPH ? prepare_correction<SPH>(*c, out) : (G == CYL ? prepare_correction<CYL>(*c, out) : prepare_correction<CART>(*c, out));
-        if (rc) return rc;
-    }
+    int rc = ensure_correction(*c);
+    if (rc) return rc;
     CK(cudaEventRecord(c->ev0, c->stream));
     const int chunk = 100;
     for (int64_t done = 0; done < k;) {
@@ -1835,6 +1875,7 @@ int sph_sweep(void* h, int64_t k) {
 int sph_residual_fields(void* h, double* rV1, double* rV2, double* rV3, double* rP) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     int rc = sync64(*c);
     if (rc) return rc;
     double out[7];
@@ -1855,6 +1896,7 @@ int sph_residual_vjp(void* h, const double* lV1, const double* lV2, const double
                      double* aV3, double* aP, double* g_eta, double* g_rho, int32_t flags) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     int rc = sync64(*c);
     if (rc || (rc = adj_alloc(c))) return rc;
     if ((rc = adj_upload(c, AJ_LV1, SPH_FIELD_V1, lV1)) || (rc = adj_upload(c, AJ_LV2, SPH_FIELD_V2, lV2)) ||
@@ -1877,6 +1919,7 @@ int sph_residual_vjp(void* h, const double* lV1, const double* lV2, const double
 int sph_advect(void* h, double dt, double delta, int32_t nf, const double* const* phi, double* const* phi_new) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || (nf > 0 && (!phi || !phi_new))) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (nf < 1 || nf > 4) return fail(SPH_ERR_INVALID, "sph_advect: 1 to 4 fields");
     int rc = sync64(*c);
     if (rc || (rc = adj_alloc(c))) return rc;
@@ -1902,6 +1945,7 @@ int sph_advect_vjp(void* h, double dt, double delta, int32_t nf, const double* c
                    double* aV1, double* aV2, double* aV3) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !phi || !mu_new || !mu) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (nf < 1 || nf > 4) return fail(SPH_ERR_INVALID, "sph_advect_vjp: 1 to 4 fields");
     int rc = sync64(*c);
     if (rc || (rc = adj_alloc(c))) return rc;
@@ -1934,6 +1978,7 @@ int sph_advect_vjp(void* h, double dt, double delta, int32_t nf, const double* c
 int sph_bc_vjp(void* h, double* aV1, double* aV2, double* aV3) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !aV1 || !aV2 || !aV3) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     int rc = sync64(*c);
     if (rc || (rc = adj_alloc(c))) return rc;
     if ((rc = adj_upload(c, AJ_V1, SPH_FIELD_V1, aV1)) || (rc = adj_upload(c, AJ_V2, SPH_FIELD_V2, aV2)) ||
@@ -1961,6 +2006,7 @@ int sph_bc_vjp(void* h, double* aV1, double* aV2, double* aV3) {
 int sph_residual_vjp_law(void* h, double* g_eta_ini, double* g_n) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (!c->adj) return fail(SPH_ERR_INVALID, "sph_residual_vjp_law: no sph_residual_vjp before");
     int rc = adj_download(c, AJ_GEI, SPH_FIELD_P, g_eta_ini);
     if (rc) return rc;
@@ -1979,6 +2025,7 @@ int sph_adjoint_solve(void* h, const double* bV1, const double* bV2, const doubl
                       double* lV3, double* lP, const sph_solve_opts* o, sph_solve_info* info) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !o || !lV1 || !lV2 || !lV3 || !lP) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (o->tol <= 0.0 || o->maxiter <= 0) return fail(SPH_ERR_INVALID, "tol and maxiter must be positive");
     int rc = sync64(*c);
     if (rc || (rc = adj_alloc(c))) return rc;
@@ -2007,6 +2054,7 @@ int sph_save(void* h, const char* dir, int32_t num, double tol, double runtime_s
              int64_t nhist) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !dir) return fail(SPH_ERR_INVALID, "sph_save: NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (nhist < 0 || (nhist > 0 && (!hist_iter || !hist_err))) return fail(SPH_ERR_INVALID, "sph_save: history");
     int rc = sync64(*c);
     if (rc) return rc;
@@ -2091,6 +2139,7 @@ int sph_save(void* h, const char* dir, int32_t num, double tol, double runtime_s
 int sph_sweep_profile(void* h, int64_t k, double* sweep_ms, double* kernel_ms) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !sweep_ms || !kernel_ms) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     if (k < 0) return fail(SPH_ERR_INVALID, "k < 0");
     if (!c->fused) return fail(SPH_ERR_UNSUPPORTED, "sph_sweep_profile times the fused sweep kernel (SPH_KERNELS_AUTO)");
     *sweep_ms = 0.0;
@@ -2137,6 +2186,7 @@ int sph_sweep_profile(void* h, int64_t k, double* sweep_ms, double* kernel_ms) {
 int sph_sweep_apply(void* h) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (!c->corr_ready) return SPH_OK;
     int rc = apply_correction(*c);
     if (rc) return rc;
@@ -2144,9 +2194,64 @@ int sph_sweep_apply(void* h) {
     return SPH_OK;
 }
 
+// FP32 slot and reference-layout extent of a correction-problem field (sph_corr_field)
+static int corr_slot(const Ctx* c, int32_t field, int e[3]) {
+    static const int slots[SPH_CORR_COUNT] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23,
+                                              F_ETA, F_ETA_SM, F_RP, F_RV1, F_RV2, F_RV3};
+    static const int shape[SPH_CORR_COUNT] = {SPH_FIELD_P, SPH_FIELD_V1, SPH_FIELD_V2, SPH_FIELD_V3, SPH_FIELD_TAU11,
+                                              SPH_FIELD_TAU22, SPH_FIELD_TAU33, SPH_FIELD_TAU12, SPH_FIELD_TAU13, SPH_FIELD_TAU23,
+                                              SPH_FIELD_P, SPH_FIELD_P, SPH_FIELD_P, SPH_FIELD_V1, SPH_FIELD_V2, SPH_FIELD_V3};
+    if (field < 0 || field >= SPH_CORR_COUNT) return -1;
+    field_extent(c->d, shape[field], e);
+    return slots[field];
+}
+
+static int corr_access(void* h, int32_t field, double* host, const double* src, int64_t count) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
+    if (c->prm.precision != SPH_PREC_MIXED) return fail(SPH_ERR_UNSUPPORTED, "the correction problem exists in SPH_PREC_MIXED only");
+    if (c->prm.rheology == SPH_RHEO_TAU_POWER || c->prm.rheology == SPH_RHEO_TAU_POWER_RELAX)
+        return fail(SPH_ERR_UNSUPPORTED, "mixed precision needs an explicit viscosity law (linear or strain-rate power law)");
+    if (!host && !src) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    int e[3];
+    const int slot = corr_slot(c, field, e);
+    if (slot < 0) return fail(SPH_ERR_INVALID, "correction field");
+    if (count != (int64_t)e[0] * e[1] * e[2]) return fail(SPH_ERR_INVALID, "count does not match the field size");
+    int rc = ensure_correction(*c);
+    if (rc) return rc;
+    float* dev = c->s32.f[slot];
+    return host ? download_box<float>(*c, dev, e, host) : upload_box<float>(*c, dev, e, src);
+}
+
+int sph_corr_get(void* h, int32_t field, double* host, int64_t count) {
+    if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    return corr_access(h, field, host, nullptr, count);
+}
+
+int sph_corr_set(void* h, int32_t field, const double* host, int64_t count) {
+    if (!host) return fail(SPH_ERR_INVALID, "host pointer is NULL");
+    return corr_access(h, field, nullptr, host, count);
+}
+
+int sph_selftest_wait_timeout(void* h) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
+    if (!c->d_err) {
+        if (cudaMalloc((void**)&c->d_err, sizeof(int)) != cudaSuccess) return fail(SPH_ERR_NOMEM, "error word");
+        CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->stream));
+    }
+    // 1000 polls of at most 1 us each: the wait runs out within a few milliseconds
+    k_wait_selftest<<<1, 32, 0, c->stream>>>(c->d_err, 1000, 1000u);
+    CK(cudaGetLastError());
+    return check_kernel_flag(*c);
+}
+
 int sph_residual(void* h, double out[7]) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c || !out) return fail(SPH_ERR_INVALID, "NULL argument");
+    if (int rc_ = usable(*c)) return rc_;
     int rc = sync64(*c);
     if (rc) return rc;
     return residual64(*c, out);
@@ -2155,6 +2260,7 @@ int sph_residual(void* h, double out[7]) {
 int sph_run_kernel(void* h, int32_t kernel) {
     Ctx* c = static_cast<Ctx*>(h);
     if (!c) return fail(SPH_ERR_INVALID, "ctx is NULL");
+    if (int rc_ = usable(*c)) return rc_;
     if (c->prm.precision != SPH_PREC_FP64) return fail(SPH_ERR_UNSUPPORTED, "single kernels run on the FP64 state");
     int rc = sync64(*c);
     if (rc) return rc;
@@ -2185,6 +2291,14 @@ int sph_run_kernel(void* h, int32_t kernel) {
     }
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(c->stream));
+    return SPH_OK;
+}
+
+int sph_solve_history_ms(void* h, double* ms, int64_t cap, int64_t* n) {
+    Ctx* c = static_cast<Ctx*>(h);
+    if (!c || !n || (cap > 0 && !ms)) return fail(SPH_ERR_INVALID, "NULL argument");
+    *n = (int64_t)c->hist_ms.size();
+    for (int64_t i = 0; i < cap && i < *n; ++i) ms[i] = c->hist_ms[(size_t)i];
     return SPH_OK;
 }
 

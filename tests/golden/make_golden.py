@@ -568,7 +568,9 @@ def run_case(ref: Path, name: str):
 
 
 def main():
-    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: make_golden.py <path of the SphericalStokes checkout> [case ...]")
+    ref = Path(sys.argv[1])
     names = sys.argv[2:] or list(CASES)
     for n in names:
         run_case(ref, n)

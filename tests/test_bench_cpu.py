@@ -1,0 +1,50 @@
+"""bench.py's reference arm on CPU: its workload equals the library arm's, it never maps the
+product library, and its line carries the same ``config`` as the library arm's."""
+import json
+import math
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+sys.path.insert(0, str(ROOT))
+
+import bench  # noqa: E402
+
+
+KEYS = ("geometry", "bc", "rheology", "init", "n1", "n2", "n3", "c1", "c2", "c3", "l1", "l2", "l3", "l_ref", "vpdt", "dmp",
+        "g", "tau_C", "n_exp", "relax", "edot_bg", "r", "sh", "eta0", "vr", "rho0", "rho_in", "radius", "incl_linear",
+        "etasm_passes")
+
+
+@pytest.mark.parametrize("n", [31, 255])
+def test_reference_workload_equals_library_workload(n):
+    lib = bench.workload_params(n, "fp64")
+    ref = bench.reference_params(n)
+    for k in KEYS:
+        assert getattr(ref, k) == pytest.approx(getattr(lib, k), rel=1e-15, abs=0.0), k
+    assert tuple(ref.sig_bc) == tuple(lib.sig_bc)
+
+
+def test_reference_sample_keeps_the_spacing():
+    full, _ = bench.reference_workload(31)
+    sample, _ = bench.reference_workload(31, 9)
+    assert sample.n3 == 9 and sample.vpdt == full.vpdt
+    assert sample.l3 / (sample.n3 - 1) == pytest.approx(full.l3 / (full.n3 - 1), rel=1e-15)
+    assert math.isclose(sample.c3, 0.0)
+
+
+def test_reference_arm_does_not_map_the_product_library():
+    code = ("import sys; sys.argv=['bench.py','--impl','reference','--n','23','--steps','2','--warmup','1',"
+            "'--ref-seconds','0.5']; import bench; bench.main(); "
+            "print('MAPPED', open('/proc/self/maps').read().count('libsphstokes'))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.strip().splitlines()
+    line = json.loads(lines[0])
+    assert lines[-1] == "MAPPED 0"
+    assert line["impl"] == "reference" and line["config"] == bench.workload_config(23)
+    assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["ms_per_iteration"] > 0 and line["word_bytes"] == 8

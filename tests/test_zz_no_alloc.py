@@ -61,3 +61,17 @@ def test_check_err_noalloc_rejects_more_arrays_than_its_scratch():
     assert "holds 1 to 8" in lib.sph_last_error().decode()
     rc, err = _check_err(lib, torch, [a] * 8, [a] * 8)  # at the maximum: fine, no change -> 0
     assert rc == S.SPH_OK and err == 0.0
+
+
+def test_check_err_noalloc_propagates_nan():
+    """A NaN in a snapshot makes err NaN, as Julia's maximum(abs.(.)) ratio does (a caller's
+    isnan(err) divergence guard then fires), and a later call without NaN is finite again."""
+    torch = pytest.importorskip("torch")
+    lib = S.load_library()
+    v = torch.linspace(1.0, 2.0, 1000, dtype=torch.float64, device="cuda")
+    old = v.clone()
+    old[123] = float("nan")
+    rc, err = _check_err(lib, torch, [v, v], [v.clone(), old])
+    assert rc == S.SPH_OK and np.isnan(err)
+    rc, err = _check_err(lib, torch, [v], [v * 0.5])
+    assert rc == S.SPH_OK and err == pytest.approx(0.5, rel=1e-15)

@@ -215,6 +215,17 @@ class Sph:
         L.orc_sph_corr_sweep.argtypes = [C.POINTER(SphState), C.POINTER(SphParams), _PD, _PD, _PD, _PD, C.c_int64]
         L.orc_sph_corr_sweep(C.byref(self.st), C.byref(self.prm), *[_ptr(a) for a in rhs], int(k))
 
+    def residual_fields(self) -> dict:
+        """The residual's fields (orc_sph_residual): momentum rows rV1..rV3 (velocity shapes, zero
+        outside the interior nodes) and rP = div V (cells)."""
+        nr, nt, np_ = self.n
+        scr = np.zeros(int(lib().orc_sph_residual_scratch_size(nr, nt, np_)), dtype=np.float64)
+        out = np.zeros(5, dtype=np.float64)
+        f = {k: np.zeros(self.field(k).shape, dtype=np.float64, order="F") for k in ("V1", "V2", "V3", "P")}
+        lib().orc_sph_residual(C.byref(self.st), C.byref(self.prm), _ptr(out), _ptr(scr), _ptr(f["V1"]), _ptr(f["V2"]),
+                               _ptr(f["V3"]), _ptr(f["P"]))
+        return f
+
     def residual(self, f_scale: float | None = None) -> dict:
         nr, nt, np_ = self.n
         scr = np.zeros(int(lib().orc_sph_residual_scratch_size(nr, nt, np_)), dtype=np.float64)

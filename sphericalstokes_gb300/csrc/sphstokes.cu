@@ -1833,7 +1833,9 @@ int sph_solve(void* h, const sph_solve_opts* o, sph_solve_info* info, int64_t* h
     inf->device_ms = ms;
     inf->sweep_ms = prec == SPH_PREC_MIXED ? c->sweep_ms : ms;
     inf->outer_ms = c->outer_ms;
-    {
+    // the FP64 residual of the final state: the mixed solve's last outer step evaluated it (its
+    // loop ends right after a residual evaluation; the final P and τ copies leave it unchanged)
+    if (prec != SPH_PREC_MIXED) {
         rc = sync64(*c);
         if (rc) return rc;
         double out[7];

@@ -63,8 +63,11 @@ def run_case(p, k, random_start, seed=0):
     err = {}
     for g, fs in GROUPS.items():
         scale = max(float(np.abs(o.field(ORACLE_NAME[f])).max()) for f in fs)
-        assert scale > 0.0, (g, "the oracle's correction is zero: the case exercises nothing")
-        err[g] = max(float(np.abs(got[f] - o.field(ORACLE_NAME[f])).max()) for f in fs) / scale
+        diff = max(float(np.abs(got[f] - o.field(ORACLE_NAME[f])).max()) for f in fs)
+        # a group the oracle leaves exactly zero (δP and δτ after one sweep from a zero correction
+        # with rP = 0) must be exactly zero on the GPU too
+        err[g] = diff / scale if scale > 0.0 else (0.0 if diff == 0.0 else float("inf"))
+    assert any(float(np.abs(o.field(ORACLE_NAME[f])).max()) > 0.0 for f in STATE), "the case exercises nothing"
     return err
 
 

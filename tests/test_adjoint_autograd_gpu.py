@@ -32,6 +32,8 @@ def _state(sv, rng, law):
     st["ETA_INI" if law else "ETA"] = np.asfortranarray(np.exp(rng.uniform(-1.0, 1.0, sv.dims("P"))))
     for f, a in st.items():
         sv.set(f, a)
+    if law:  # about a fifth of the cells linear (phase 1), the rest on the power law
+        sv.set("PHASE", np.asfortranarray((rng.uniform(size=sv.dims("P")) < 0.2).astype(np.float64)))
     return st
 
 

@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 1
+#define SPH_ABI_VERSION 2
 
 typedef enum sph_status {
     SPH_OK = 0,
@@ -178,7 +178,14 @@ typedef struct sph_solve_info {
     double device_ms;      /* device time of the solve (CUDA events on the context's stream) */
     double sweep_ms;       /* of which PT sweeps (MIXED: the FP32 correction sweeps) */
     double outer_ms;       /* of which FP64 outer work (MIXED: residual, coefficients) */
+    int32_t flags;         /* SPH_SOLVE_WARM_ABANDONED: the FP32 warm start produced a NaN or an
+                              infinite error and was abandoned (the correction loop started from the
+                              FP64 state as it was; its iterations count in iters) */
+    int32_t reserved_i;
+    double reserved[3];
 } sph_solve_info;
+
+#define SPH_SOLVE_WARM_ABANDONED 1
 
 /* defaults of the reference script of the given geometry (diapir setups) */
 int sph_params_default(sph_params* p, int32_t geometry);

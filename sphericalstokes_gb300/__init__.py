@@ -91,7 +91,11 @@ class SolveInfo(C.Structure):
         ("iters", C.c_int64), ("outer", C.c_int32), ("status", C.c_int32), ("err", C.c_double),
         ("residual", C.c_double), ("seconds", C.c_double), ("nhist", C.c_int64),
         ("device_ms", C.c_double), ("sweep_ms", C.c_double), ("outer_ms", C.c_double),
+        ("flags", C.c_int32), ("reserved_i", C.c_int32), ("reserved", C.c_double * 3),
     ]
+
+
+SPH_SOLVE_WARM_ABANDONED = 1
 
 
 # every symbol include/sphstokes.h declares, with its ctypes signature
@@ -213,6 +217,11 @@ class SolveResult:
     device_ms: float = 0.0
     sweep_ms: float = 0.0
     outer_ms: float = 0.0
+    flags: int = 0
+
+    @property
+    def warm_abandoned(self) -> bool:
+        return bool(self.flags & SPH_SOLVE_WARM_ABANDONED)
 
     @property
     def converged(self) -> bool:
@@ -320,7 +329,7 @@ class Solver:
         n = int(info.nhist)
         return SolveResult(int(info.status), int(info.iters), int(info.outer), float(info.err), float(info.residual),
                            float(info.seconds), hi[:n].copy(), he[:n].copy(), float(info.device_ms), float(info.sweep_ms),
-                           float(info.outer_ms))
+                           float(info.outer_ms), int(info.flags))
 
     def history_ms(self) -> np.ndarray:
         """Wall-clock ms from the start of the last solve to each of its history entries."""
@@ -439,4 +448,4 @@ def solve_batch(solvers: list, opts: list | SolveOpts, threads: int = 0) -> list
     _check(lib, lib.sph_batch_solve(ctxs, n, oa, ia, int(threads)), "sph_batch_solve")
     empty_i, empty_e = np.zeros(0, dtype=np.int64), np.zeros(0)
     return [SolveResult(int(x.status), int(x.iters), int(x.outer), float(x.err), float(x.residual), float(x.seconds),
-                        empty_i, empty_e, float(x.device_ms), float(x.sweep_ms), float(x.outer_ms)) for x in ia]
+                        empty_i, empty_e, float(x.device_ms), float(x.sweep_ms), float(x.outer_ms), int(x.flags)) for x in ia]

@@ -118,6 +118,7 @@ struct Ctx {
     int* d_err = nullptr;                // set by a kernel whose bounded wait ran out
     bool use_tma = true;
     bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
+    bool use_deep = false;  // k_fused_tma with the three-slot old-state ring, rP and rV read per thread
     bool use_pdl = true;  // sweep and BC kernels launched with a programmatic dependency (pdl_enter)
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep (0: chosen by fused_chunk())
@@ -133,6 +134,7 @@ struct Ctx {
     std::vector<double> hist_ms;
     std::chrono::steady_clock::time_point solve_t0;
     bool broken = false;      // a bounded wait of a sweep kernel ran out: the context's state is suspect
+    bool warm_abandoned = false;  // the last mixed solve's FP32 warm start produced a NaN and was abandoned
 };
 
 constexpr int kRedSlots = 16;
@@ -557,6 +559,7 @@ int fused_chunk(const Ctx& c) {
 template <int G, int MODE>
 void set_tma_attr() {
     cudaFuncSetAttribute(k_fused_tma<G, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
+    cudaFuncSetAttribute(k_fused_tma<G, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes(true));
 }
 
 template <int G, int MODE>
@@ -996,6 +999,9 @@ void correction_sweep(Ctx& c) {
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next], c.stream);
             if (c.use_x2)
                 k_sweep_x2<G><<<grid, dim3(X2_NT, 1, 1), sweep_x2_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
+            else if (c.use_deep)
+                launch_pdl(c.use_pdl, k_fused_tma<G, 1, true>, grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(true), c.stream, q, o, kc,
+                           maps, c.d_err);
             else
                 launch_pdl(c.use_pdl, k_fused_tma<G, 1>, grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream, q, o, kc, maps, c.d_err);
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
@@ -1146,11 +1152,15 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
     int64_t iters = 0;
     int status = SPH_ERR_NOT_CONVERGED;
     double err = 1.0;
-    // optional FP32 nonlinear warm start on the full variables
+    c.warm_abandoned = false;
+    // optional FP32 nonlinear warm start on the full variables.  The FP64 state is only
+    // overwritten once it succeeds: a warm start whose FP32 iteration produces a NaN is
+    // abandoned and the correction loop starts from the FP64 state as it was.
     if (o.warm_tol > 0.0) {
         int rc = sync32(c);
         if (rc) return rc;
         double werr = 1.0;
+        bool warm_ok = true;
         while (iters < o.maxiter) {
             // the plain iterations up to the next check, replayed from a graph
             const int64_t before = nout - 1 - (iters % nout);
@@ -1168,16 +1178,19 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
             if (!check) continue;
             rc = ref_err<float>(c, t, &werr, false);
             if (rc) return rc;
-            if (!(werr == werr)) return fail(SPH_ERR_DIVERGED, "NaN in the FP32 warm start");
+            if (!(werr == werr) || std::isinf(werr)) { warm_ok = false; break; }
             if (werr < o.warm_tol && iters > 20) break;
         }
-        // widen V, P (η is recomputed from the law)
-        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
-        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
-        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
-        k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
-        if (!law) k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_ETA], t.f[F_ETA], vol);
-        CK(cudaGetLastError());
+        if (warm_ok) {  // widen V, P (η is recomputed from the law)
+            k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V1], t.f[F_V1], vol);
+            k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V2], t.f[F_V2], vol);
+            k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_V3], t.f[F_V3], vol);
+            k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_P], t.f[F_P], vol);
+            if (!law) k_convert<double, float><<<ew_blocks(vol), 256, 0, c.stream>>>(s.f[F_ETA], t.f[F_ETA], vol);
+            CK(cudaGetLastError());
+        }
+        c.warm_abandoned = !warm_ok;
+        c.stale32 = true;  // the FP32 state holds the warm start's iterate, not the FP64 state
     }
     float ms = 0.f;
     for (int outer = 0; outer <= o.max_outer; ++outer) {
@@ -1242,7 +1255,10 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
     }
     c.stale32 = true;
     c.stale64 = false;
-    if (info) { info->iters = iters; info->err = err; info->status = status; }
+    if (info) {
+        info->iters = iters; info->err = err; info->status = status;
+        if (c.warm_abandoned) info->flags |= SPH_SOLVE_WARM_ABANDONED;
+    }
     return SPH_OK;
 }
 
@@ -1393,6 +1409,7 @@ int sph_create(const sph_params* prm, void** out) {
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
+    if (const char* e = std::getenv("SPH_SWEEP_DEEP")) c->use_deep = std::atoi(e) != 0;
     if (const char* e = std::getenv("SPH_NO_PDL")) c->use_pdl = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_XGHOST")) c->xg_fuse = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);

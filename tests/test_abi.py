@@ -37,7 +37,7 @@ def test_python_binding_covers_header():
 
 def test_abi_version_and_strerror():
     lib = S.load_library()
-    assert lib.sph_abi_version() == 1
+    assert lib.sph_abi_version() == 2
     assert lib.sph_strerror(S.SPH_ERR_DIVERGED).decode().startswith("diverged")
     assert lib.sph_strerror(12345).decode() == "unknown status"
 

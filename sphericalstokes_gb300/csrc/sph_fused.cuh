@@ -292,20 +292,6 @@ struct TmaSmem {
     unsigned long long bar_in[3];
     unsigned long long bar_old[2];
 };
-// Deep variant: the old-state ring has three slots of the seven state fields (P, τ), filled two
-// planes ahead; the right-hand sides rP (stage-1 point) and rV (velocity node) are read by each
-// thread at its own point straight from global memory, issued at the start of the plane's step.
-struct TmaSmemDeep {
-    alignas(128) float in[3][F_IN][TIN_TILE];
-    alignas(128) float old[3][7][TOLD_TILE];
-    float st[2][7][FSY][FSX];
-    unsigned long long bar_in[3];
-    unsigned long long bar_old[3];
-};
-template <bool DEEP>
-struct TmaSmemOf { using type = TmaSmem; };
-template <>
-struct TmaSmemOf<true> { using type = TmaSmemDeep; };
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -470,15 +456,12 @@ __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4,
 // step and velocities from registers.  Warp 8 computes the low-x2 halo row
 // (b = 0), lanes 0..8 of warp 9 the low-x1 halo column (a = 0).  Shared-memory
 // rows are then read by whole warps at consecutive addresses.
-template <int G, int MODE, bool DEEP = false>
+template <int G, int MODE>
 __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
                                                        int* __restrict__ err) {
-    static_assert(!DEEP || MODE == 1, "the deep variant reads rP and rV: correction problem only");
     pdl_wait();  // no early release of the next grid: its blocks would take SM slots in this grid's tail
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    using Smem = typename TmaSmemOf<DEEP>::type;
-    Smem& S = *reinterpret_cast<Smem*>(smem_raw);
-    constexpr int NOLD = DEEP ? 3 : 2;  // old-state ring slots
+    TmaSmem& S = *reinterpret_cast<TmaSmem*>(smem_raw);
     enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-tile slots (IX: rP | ρ)
     enum { Q11 = 0, Q22, Q33, E12, E13, E23, QDT };     // stress-ring slots
 
@@ -493,28 +476,25 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
 
     if (tid == 0) {
         for (int i = 0; i < 3; ++i) mbar_init(&S.bar_in[i], 1);
-        for (int i = 0; i < NOLD; ++i) mbar_init(&S.bar_old[i], 1);
+        for (int i = 0; i < 2; ++i) mbar_init(&S.bar_old[i], 1);
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
 
     const unsigned in_bytes = F_IN * TIN_X * TIN_Y * 4;
-    const unsigned old_bytes = DEEP ? 7 * TOLD_X * TOLD_Y * 4 : F_OLD * TOLD_X * TOLD_Y * 4 + (MODE == 1 ? F_RV * FTX * FTY * 4 : 0);
-    auto old_slot = [](int z) { return DEEP ? (z + 3) % 3 : (z & 1); };
+    const unsigned old_bytes = F_OLD * TOLD_X * TOLD_Y * 4 + (MODE == 1 ? F_RV * FTX * FTY * 4 : 0);
     auto issue_inputs = [&](int z) {  // thread 0 only
         const int sl = (z + 3) % 3;
         mbar_expect_tx(&S.bar_in[sl], in_bytes);
         for (int f = 0; f < F_IN; ++f) tma_load3d(S.in[sl][f], maps + TM_V1 + f, x0 - 4, y0 - 1, z, &S.bar_in[sl]);
     };
-    auto issue_old = [&](int z) {  // thread 0 only: old state (+ rP and rV of plane z unless DEEP)
-        const int sl = old_slot(z);
+    auto issue_old = [&](int z) {  // thread 0 only: old state + rV of plane z
+        const int sl = z & 1;
         mbar_expect_tx(&S.bar_old[sl], old_bytes);
         for (int f = 0; f < 7; ++f) tma_load3d(S.old[sl][f], maps + TM_P + f, x0 - 4, y0 - 1, z, &S.bar_old[sl]);
-        if constexpr (!DEEP) {
-            tma_load3d(S.old[sl][IX], maps + (MODE == 1 ? TM_RP : TM_RHO), x0 - 4, y0 - 1, z, &S.bar_old[sl]);
-            if (MODE == 1)
-                for (int f = 0; f < F_RV; ++f) tma_load3d(S.rv[sl][f], maps + TM_RV1 + f, x0, y0, z, &S.bar_old[sl]);
-        }
+        tma_load3d(S.old[sl][IX], maps + (MODE == 1 ? TM_RP : TM_RHO), x0 - 4, y0 - 1, z, &S.bar_old[sl]);
+        if (MODE == 1)
+            for (int f = 0; f < F_RV; ++f) tma_load3d(S.rv[sl][f], maps + TM_RV1 + f, x0, y0, z, &S.bar_old[sl]);
     };
     unsigned ph_in = 0, ph_old = 0;  // parity bit per ring slot
     // false once a bounded wait ran out: from then on this thread neither waits nor (thread 0)
@@ -528,7 +508,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     };
     auto wait_old = [&](int z) {
         if (!ok) return;
-        const int sl = old_slot(z);
+        const int sl = z & 1;
         ok = mbar_wait(&S.bar_old[sl], (ph_old >> sl) & 1u);
         ph_old ^= 1u << sl;
     };
@@ -560,15 +540,14 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     const float gsc4 = 0.25f * gsc;
     // stage1 / velocity of an interior plane (1 <= k <= n3 - 3: every x3 condition holds
     // and no x3 face is a traction face) when `inner` is std::true_type
-    // rp: rP of this thread's stage-1 point (DEEP only; the old-state tile holds it otherwise)
-    auto stage1 = [&](int k, bool own_plane, int sk, auto inner, float rp) {
+    auto stage1 = [&](int k, bool own_plane, int sk, auto inner) {
         constexpr bool IN = decltype(inner)::value;
         if (!s1_thread) return;
         const float* I0 = S.in[sk][0] + iin;
         const float* I1 = S.in[sk == 2 ? 0 : sk + 1][0] + iin;
         auto in0 = [&](int f, int db, int da) { return I0[f * TIN_TILE + db * TIN_X + da]; };
         auto in1 = [&](int f, int db, int da) { return I1[f * TIN_TILE + db * TIN_X + da]; };
-        const float* O = &S.old[old_slot(k)][0][0] + iold;
+        const float* O = &S.old[k & 1][0][0] + iold;
         auto old = [&](int f) { return O[f * TOLD_TILE]; };
         const bool own = own_plane && s1_own;
         const int g = gxy + d.sz * k;
@@ -584,8 +563,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
             const float gs = gsc * sm, kb = kbc * sm;
             const float f = pdiv(e, e + gs);
             float dv = D.div;
-            if constexpr (DEEP) dv += rp;
-            else if (MODE == 1) dv += old(IX);
+            if (MODE == 1) dv += old(IX);
             vP = old(IP) - kb * dv;
             v11 = (old(I11) + 2.f * gs * D.D11) * f;
             v22 = (old(I22) + 2.f * gs * D.D22) * f;
@@ -627,9 +605,8 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         W[E12][b][a] = v12; W[E13][b][a] = v13; W[E23][b][a] = v23; W[QDT][b][a] = vdt;
     };
 
-    // velocities of plane K from the stresses of planes K-1 and K (rv: rV at this thread's
-    // velocity node, DEEP only)
-    auto velocity = [&](int K, auto inner, const float* rv) {
+    // velocities of plane K from the stresses of planes K-1 and K
+    auto velocity = [&](int K, auto inner) {
         constexpr bool IN = decltype(inner)::value;
         if (warp >= FTY) return;
         float (*C0)[FSY][FSX] = S.st[K & 1];
@@ -649,11 +626,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
                                         c23, p23);
             // V3 (I, J, K-1/2), cell m = (I, J, K-1)
             float r3 = sw_mom3<G>(sc, d1, p33, o33, C1[E13][ty][tx + 1], p13, C1[E23][ty + 1][tx], p23);
-            if constexpr (DEEP) {
-                r1 += rv[0];
-                r2 += rv[1];
-                r3 += rv[2];
-            } else if (MODE == 1) {
+            if (MODE == 1) {
                 r1 += S.rv[K & 1][0][ty * FTX + tx];
                 r2 += S.rv[K & 1][1][ty * FTX + tx];
                 r3 += S.rv[K & 1][2][ty * FTX + tx];
@@ -678,29 +651,15 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         p13 = c13; p23 = c23; p33 = o33; pdt = odt;
     };
 
-    // rP and rV at this thread's points of plane z (DEEP): plain loads, issued before the waits
-    // of the plane's step so that their latency overlaps the barrier and the stage-1 work
-    const bool rv_ok = warp < FTY && I < d.px && J < d.py;
-    auto load_rp = [&](int z) { return (DEEP && s1_in && z >= 0 && z < n3) ? __ldg(p.rP + gxy + d.sz * z) : 0.f; };
-    auto load_rv = [&](int z, float* rv) {
-        const int g = gIJ + d.sz * z;
-        const bool okz = DEEP && rv_ok && z >= 0 && z < d.pz;
-        rv[0] = okz ? __ldg(p.rV1 + g) : 0.f;
-        rv[1] = okz ? __ldg(p.rV2 + g) : 0.f;
-        rv[2] = okz ? __ldg(p.rV3 + g) : 0.f;
-    };
-
-    // prologue: inputs kA-1, kA, kA+1; old kA-1, kA (and kA+1 when DEEP)
+    // prologue: inputs kA-1, kA, kA+1; old kA-1, kA
     if (tid == 0) {
         issue_inputs(kA - 1);
         issue_inputs(kA);
         issue_old(kA - 1);
         issue_inputs(kA + 1);
         issue_old(kA);
-        if (DEEP && kA + 1 <= kB - 1) issue_old(kA + 1);
     }
     const bool waiter = warp == 0;
-    const float rp0 = load_rp(kA - 1);
     if (waiter) {
         wait_in(kA - 1);
         wait_in(kA);
@@ -709,14 +668,11 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     __syncthreads();
     int sk = (kA + 2) % 3;  // input-ring slot of plane kA - 1
     if (kA >= 1) {
-        stage1(kA - 1, false, sk, std::false_type{}, rp0);
+        stage1(kA - 1, false, sk, std::false_type{});
         p33 = o33;
         pdt = odt;
     }
     auto step = [&](int K, auto inner) {
-        float rv[3];
-        const float rp = load_rp(K);
-        load_rv(K, rv);
         if (waiter) {
             wait_in(K + 1);
             wait_old(K);
@@ -724,12 +680,12 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
         __syncthreads();  // every thread is done with the slots of plane K-1; inputs K+1 and old K have landed
         if (tid == 0 && ok) {  // only planes the chunk uses: inputs up to kB, old state and rV up to kB - 1
             if (K + 2 <= kB) issue_inputs(K + 2);
-            if (K + NOLD - 1 <= kB - 1) issue_old(K + NOLD - 1);
+            if (K + 1 <= kB - 1) issue_old(K + 1);
         }
         sk = sk == 2 ? 0 : sk + 1;
-        stage1(K, true, sk, inner, rp);
+        stage1(K, true, sk, inner);
         __syncthreads();
-        velocity(K, inner, rv);
+        velocity(K, inner);
     };
     step(kA, std::false_type{});  // (sets the carried edge stresses of plane kA - 1)
     for (int K = kA + 1; K < kB; ++K) {
@@ -743,6 +699,6 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     if (waiter && !ok && err) atomicExch(err, 1);
 }
 
-inline size_t fused_tma_smem_bytes(bool deep = false) { return deep ? sizeof(TmaSmemDeep) : sizeof(TmaSmem); }
+inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }
 
 }  // namespace sph

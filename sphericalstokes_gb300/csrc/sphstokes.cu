@@ -118,7 +118,6 @@ struct Ctx {
     int* d_err = nullptr;                // set by a kernel whose bounded wait ran out
     bool use_tma = true;
     bool use_x2 = false;  // TMA sweep with two points per thread (k_sweep_x2) instead of k_fused_tma
-    bool use_deep = false;  // k_fused_tma with the three-slot old-state ring, rP and rV read per thread
     bool use_pdl = true;  // sweep and BC kernels launched with a programmatic dependency (pdl_enter)
     bool fused = true;   // FP32 sweeps use the fused kernel
     int fused_chunk = 0; // planes per block of the fused sweep (0: chosen by fused_chunk())
@@ -559,7 +558,6 @@ int fused_chunk(const Ctx& c) {
 template <int G, int MODE>
 void set_tma_attr() {
     cudaFuncSetAttribute(k_fused_tma<G, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
-    cudaFuncSetAttribute(k_fused_tma<G, MODE, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes(true));
 }
 
 template <int G, int MODE>
@@ -999,9 +997,6 @@ void correction_sweep(Ctx& c) {
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next], c.stream);
             if (c.use_x2)
                 k_sweep_x2<G><<<grid, dim3(X2_NT, 1, 1), sweep_x2_smem_bytes(), c.stream>>>(q, o, kc, maps, c.d_err);
-            else if (c.use_deep)
-                launch_pdl(c.use_pdl, k_fused_tma<G, 1, true>, grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(true), c.stream, q, o, kc,
-                           maps, c.d_err);
             else
                 launch_pdl(c.use_pdl, k_fused_tma<G, 1>, grid, dim3(FNT, 1, 1), fused_tma_smem_bytes(), c.stream, q, o, kc, maps, c.d_err);
             if (prof) cudaEventRecord(c.prof_ev[2 * c.prof_next++ + 1], c.stream);
@@ -1409,7 +1404,6 @@ int sph_create(const sph_params* prm, void** out) {
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
-    if (const char* e = std::getenv("SPH_SWEEP_DEEP")) c->use_deep = std::atoi(e) != 0;
     if (const char* e = std::getenv("SPH_NO_PDL")) c->use_pdl = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_XGHOST")) c->xg_fuse = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);

@@ -112,23 +112,3 @@ def test_correction_sweeps_255_slab_match_oracle():
         del os.environ["SPH_FUSED_CHUNK"]
     assert max(err.values()) < TOL, err
 
-
-@pytest.mark.parametrize("geometry,n,bc", CASES[:2] + CASES[3:])
-def test_deep_ring_variant_equals_default_sweep(geometry, n, bc):
-    """The fused sweep with the three-slot old-state ring and per-thread rP / rV loads
-    (SPH_SWEEP_DEEP=1) computes the same sweeps, bit for bit, as the default kernel."""
-    p = case_params(geometry, n, bc)
-    out = {}
-    for deep in ("0", "1"):
-        os.environ["SPH_SWEEP_DEEP"] = deep
-        try:
-            with S.Solver(p) as sv:
-                rng = np.random.default_rng(5)
-                for f in STATE:
-                    sv.corr_set(f, 1e-2 * rng.standard_normal(sv.corr_get(f).shape))
-                sv.sweep(30)
-                out[deep] = {f: sv.corr_get(f) for f in STATE}
-        finally:
-            del os.environ["SPH_SWEEP_DEEP"]
-    for f in STATE:
-        assert np.array_equal(out["0"][f], out["1"][f]), f

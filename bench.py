@@ -434,6 +434,17 @@ def run_ours(args) -> None:
 
     if args.solve_n:
         solve_info = time_to_tolerance(args)
+    # plain FP64 PT (one kernel per reference step) on the same workload: its time per iteration,
+    # the per-iteration baseline of the mixed-precision solve's FP32 sweep
+    fp64_info = None
+    if args.fp64_iters > 0:
+        with S.Solver(workload_params(n, "fp64")) as sv:
+            sv.step(2)
+            ms64 = sv.step(args.fp64_iters) / args.fp64_iters
+        fp64_info = {"ms_per_iteration": round(ms64, 4), "iterations": args.fp64_iters,
+                     "teff_gbs_fp64": round(S.teff_bytes(n, n, n, 8) / (ms64 * 1e-3) / 1e9, 2),
+                     "fp32_sweep_speedup": round(ms64 / out["ms_per_step"], 2)}
+
     plateau_info = None
     if args.plateau_sweeps > 0:
         from sphericalstokes_gb300 import plateau as PL
@@ -494,6 +505,8 @@ def run_ours(args) -> None:
         line["batch"] = batch_info
     if plateau_info:
         line["plateau_511x255x255"] = plateau_info
+    if fp64_info:
+        line["fp64_pt"] = fp64_info
     if not args.no_cpu and world == 1:
         line["cpu_baseline"] = cpu_baseline(n, seconds=args.cpu_seconds)
     print(json.dumps(line), flush=True)
@@ -513,6 +526,8 @@ def main():
     ap.add_argument("--fp64-budget-s", type=float, default=0.0,
                     help="cap plain FP64 PT of the time-to-tolerance leg at about this many seconds (0: run to 1e-8)")
     ap.add_argument("--fp64-nout", type=int, default=1000, help="FP64 residual checks every this many iterations")
+    ap.add_argument("--fp64-iters", type=int, default=5,
+                    help="plain FP64 PT iterations timed on the same workload (the FP32 sweep's per-iteration baseline; 0: skip)")
     ap.add_argument("--tuned", type=int, default=1,
                     help="time-to-tolerance PT parameters: 1 the tuned set (2 ηSM passes, 2x step, dmp 3), 0 the reference's")
     ap.add_argument("--no-cpu", action="store_true")

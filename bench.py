@@ -467,7 +467,7 @@ def run_ours(args) -> None:
         edges = tuple(int(x) for x in args.batch_edges.split(","))
         cases = B.sweep_cases(args.batch, seed=0, edges=edges)
         bo = S.make_opts(tol=1e-8, maxiter=args.batch_budget, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=30,
-                         inner_max=args.batch_budget, warm_tol=1e-5)
+                         inner_max=args.batch_budget, warm_tol=0.0)
         rb = B.run(cases, bo, threads=args.batch_threads)
         rs = B.run(cases, bo, serial=True)
         conv = sum(1 for x in rb["results"] if x.converged)

@@ -214,12 +214,19 @@ int sph_get_field(void* ctx, int32_t field, double* host, int64_t count);
 int sph_update_params(void* ctx, const sph_params* params);
 
 /* Batch of independent solves (no counterpart in the reference, which solves one grid per
- * script run): sph_solve of every context, contexts handed out to `threads` host threads
- * (<= 0: one per host core), each context on its own CUDA stream, so many small grids
- * share the GPU concurrently.  opts[i] and infos[i] belong to ctxs[i] (per-solve
- * tolerance and iteration budget in, status out); no history is recorded.  A context
- * may appear once.  Returns SPH_OK unless an argument or a CUDA call failed; the
- * outcome of each solve is infos[i].status. */
+ * script run).  opts[i] and infos[i] belong to ctxs[i] (per-solve tolerance and iteration
+ * budget in; status, iterations, outer steps and residual out); no history is recorded.  A
+ * context may appear once.  Returns SPH_OK unless an argument or a CUDA call failed; the
+ * outcome of each solve is infos[i].status.
+ *  - Lockstep batch, when every solve is SPH_PREC_MIXED on SPH_CRIT_RESIDUAL without a warm
+ *    start (warm_tol 0), with the TMA sweep and one even nout for all: the solves advance
+ *    together, and one correction sweep of all of them is one launch per geometry over a
+ *    work list of (solve, tile, x3 chunk) blocks plus one launch per BC stage, a round of
+ *    nout sweeps replayed from one CUDA graph; each solve's FP64 outer steps, inner tests
+ *    and budget are its own, and its results equal those of sph_solve alone.  infos[i].seconds
+ *    and device_ms are those of the whole batch; `threads` is not used.
+ *  - Otherwise: sph_solve of every context, handed out to `threads` host threads (<= 0: one
+ *    per host core), each context on its own CUDA stream. */
 int sph_batch_solve(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph_solve_info* infos, int32_t threads);
 
 /* Autotuner of the fused FP32 sweep (no counterpart in the reference): times `sweeps`

@@ -456,10 +456,13 @@ __device__ __forceinline__ float edge_update_q(float told, float gsc4, float s4,
 // step and velocities from registers.  Warp 8 computes the low-x2 halo row
 // (b = 0), lanes 0..8 of warp 9 the low-x1 halo column (a = 0).  Shared-memory
 // rows are then read by whole warps at consecutive addresses.
+//
+// The body takes the block's tile (bx, by) and x3 chunk (bz) as arguments, so that the
+// single-grid kernel (block indices) and the batched kernel over many grids (a work
+// list, sph_batch.cuh) run the same code.
 template <int G, int MODE>
-__global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
-                                                       int* __restrict__ err) {
-    pdl_wait();  // no early release of the next grid: its blocks would take SM slots in this grid's tail
+__device__ __forceinline__ void fused_tma_body(const KP<float>& p, const FusedOut<float>& o, int kchunk,
+                                               const CUtensorMap* __restrict__ maps, int* __restrict__ err, int bx, int by, int bz) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     TmaSmem& S = *reinterpret_cast<TmaSmem*>(smem_raw);
     enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-tile slots (IX: rP | ρ)
@@ -467,8 +470,8 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
 
     const Dims d = p.d;
     const int tid = threadIdx.x;
-    const int x0 = blockIdx.x * FTX, y0 = blockIdx.y * FTY;
-    const int kA = blockIdx.z * kchunk;
+    const int x0 = bx * FTX, y0 = by * FTY;
+    const int kA = bz * kchunk;
     const int kB = min(kA + kchunk, d.n3);
     const int n1 = d.n1, n2 = d.n2, n3 = d.n3;
     const float d1 = p.d1, d2 = p.d2, d3 = p.d3, gsc = p.gsc, kbc = p.kbc, vpdt2 = p.vpdt2;
@@ -697,6 +700,13 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<floa
     // block's shared memory as it exits and the state it wrote is suspect: the host reads the
     // flag after the launch and treats it as fatal for the context.
     if (waiter && !ok && err) atomicExch(err, 1);
+}
+
+template <int G, int MODE>
+__global__ void __launch_bounds__(FNT, 3) k_fused_tma(KP<float> p, FusedOut<float> o, int kchunk, const CUtensorMap* __restrict__ maps,
+                                                       int* __restrict__ err) {
+    pdl_wait();  // no early release of the next grid: its blocks would take SM slots in this grid's tail
+    fused_tma_body<G, MODE>(p, o, kchunk, maps, err, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 inline size_t fused_tma_smem_bytes() { return sizeof(TmaSmem); }

@@ -281,10 +281,12 @@ __global__ void __launch_bounds__(256) k_velocity(KP<T> p) {
     }
 }
 
-// max |dV + rV| of the correction problem into red[0] (inner stopping test)
+// max |dV + rV| of the correction problem over the velocity nodes of block (bx, by, bz) into
+// *red (inner stopping test); 32 x 8 threads, the body of k_velocity_norm and of its batched
+// launch over many grids
 template <typename T, int G>
-__global__ void __launch_bounds__(256) k_velocity_norm(KP<T> p) {
-    const int I = blockIdx.x * blockDim.x + threadIdx.x + 1, J = blockIdx.y * blockDim.y + threadIdx.y + 1, K = blockIdx.z + 1;
+__device__ __forceinline__ void velocity_norm_body(const KP<T>& p, int bx, int by, int bz, unsigned long long* red) {
+    const int I = bx * blockDim.x + threadIdx.x + 1, J = by * blockDim.y + threadIdx.y + 1, K = bz + 1;
     const Dims& d = p.d;
     unsigned long long m = 0ULL;  // ordered bits of the running max (NaN propagates)
     if (I <= d.n1 - 1 && J <= d.n2 - 1 && K <= d.n3 - 1) {
@@ -304,8 +306,13 @@ __global__ void __launch_bounds__(256) k_velocity_norm(KP<T> p) {
     if (w == 0) {
         m = lane < nw ? sm[lane] : 0ULL;
         for (int o = 16; o > 0; o >>= 1) m = umax64(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if (lane == 0) atomicMax(p.red, m);
+        if (lane == 0) atomicMax(red, m);
     }
+}
+
+template <typename T, int G>
+__global__ void __launch_bounds__(256) k_velocity_norm(KP<T> p) {
+    velocity_norm_body<T, G>(p, blockIdx.x, blockIdx.y, blockIdx.z, p.red);
 }
 
 // viscous stresses of the current velocities: τ_ii = 2 η D_ii at cells,
@@ -363,10 +370,10 @@ struct BcStage { int dim; int nops; BcOp op[3]; };
 template <typename T>
 __device__ __forceinline__ T* vfield(const KP<T>& p, int f) { return f == 0 ? p.V1 : (f == 1 ? p.V2 : p.V3); }
 
+// one BC stage at face point (u, v) of the stage's faces (both sides); the body of k_bc and of
+// the batched BC launch over many grids
 template <typename T, int G>
-__global__ void k_bc(KP<T> p, BcStage st, int homog) {
-    pdl_enter();
-    const int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y * blockDim.y + threadIdx.y;
+__device__ __forceinline__ void bc_body(const KP<T>& p, const BcStage& st, int homog, int u, int v) {
     const Dims& d = p.d;
     const int D = st.dim;
     const int sy = d.sy, sz = d.sz;
@@ -429,6 +436,12 @@ __global__ void k_bc(KP<T> p, BcStage st, int homog) {
             A[cb] = val;
         }
     }
+}
+
+template <typename T, int G>
+__global__ void k_bc(KP<T> p, BcStage st, int homog) {
+    pdl_enter();
+    bc_body<T, G>(p, st, homog, blockIdx.x * blockDim.x + threadIdx.x, blockIdx.y * blockDim.y + threadIdx.y);
 }
 
 // ---------------------------------------------------------------------------

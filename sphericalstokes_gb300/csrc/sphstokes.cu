@@ -32,6 +32,7 @@
 #include "sph_sweep_x2.cuh"
 #include "sph_adjoint.cuh"
 #include "sph_advect.cuh"
+#include "sph_batch.cuh"
 #include "sphstokes.h"
 
 using namespace sph;
@@ -569,6 +570,9 @@ int set_fused_attrs() {
     set_fused_attr<CYL, 0>(); set_fused_attr<CYL, 1>();
     set_fused_attr<CART, 0>(); set_fused_attr<CART, 1>();
     set_tma_attr<SPH, 1>(); set_tma_attr<CYL, 1>(); set_tma_attr<CART, 1>();
+    cudaFuncSetAttribute(k_fused_tma_batch<SPH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
+    cudaFuncSetAttribute(k_fused_tma_batch<CYL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
+    cudaFuncSetAttribute(k_fused_tma_batch<CART>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fused_tma_smem_bytes());
     cudaFuncSetAttribute(k_sweep_x2<SPH>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
     cudaFuncSetAttribute(k_sweep_x2<CYL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
     cudaFuncSetAttribute(k_sweep_x2<CART>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sweep_x2_smem_bytes());
@@ -1258,6 +1262,310 @@ int solve_mixed_g(Ctx& c, const sph_solve_opts& o, sph_solve_info* info, int64_t
 }
 
 // ---------------------------------------------------------------------------
+// Batched mixed-precision solves in lockstep (sph_batch.cuh): the per-solve sequence of
+// solve_mixed_g (FP64 outer step, preparation, correction sweeps in chunks of nout with the
+// inner test after each full chunk, FP64 update), with every full chunk of every solve run
+// as one round of batched sweeps replayed from a CUDA graph.  All work is queued on one
+// stream, so each solve's operations keep their order; results equal the solves run alone.
+struct BatchSolve {
+    Ctx* c = nullptr;
+    const sph_solve_opts* o = nullptr;
+    sph_solve_info* info = nullptr;
+    enum { OUTER, INNER, DONE } st = OUTER;
+    int64_t iters = 0;
+    int outer = 0;
+    int64_t inner = 0;
+    int status = SPH_ERR_NOT_CONVERGED;
+    double err = 1.0;
+    cudaStream_t own = nullptr;  // the context's stream, restored at the end
+};
+
+int batch_nout(const sph_solve_opts& o) { return o.nout > 0 ? o.nout : 100; }
+
+// whether a solve can run in the lockstep batch (else the batch falls back to host threads)
+bool batch_eligible(const Ctx& c, const sph_solve_opts& o) {
+    const int first = c.xg_mask ? 1 : 0;
+    return c.prm.precision == SPH_PREC_MIXED && o.criterion == SPH_CRIT_RESIDUAL && !(o.warm_tol > 0.0) &&
+           (c.prm.rheology == SPH_RHEO_LINEAR || c.prm.rheology == SPH_RHEO_EDOT_POWER_RELAX) && c.fused && c.use_tma && !c.use_x2 &&
+           !c.broken && (batch_nout(o) % 2) == 0 && o.tol > 0.0 && o.maxiter > 0 && (int)c.bc_run.size() - first <= kBatchMaxBc;
+}
+
+// the device entry of a solve whose correction problem has just been prepared
+int batch_entry(Ctx& c, BatchSweep& e) {
+    std::memset(&e, 0, sizeof(e));
+    ensure_tma_maps(c);
+    State<float>& t = c.s32;
+    for (int a = 0; a < 2; ++a) {
+        const CUtensorMap* maps = tma_maps(c);
+        if (!maps || !c.d_err) return fail(SPH_ERR_UNSUPPORTED, "batched sweeps need the TMA sweep");
+        e.p[a] = make_kp_corr(c);
+        FusedOut<float>& o = e.o[a];
+        o.P = t.f[F_A_P]; o.V1 = t.f[F_A_V1]; o.V2 = t.f[F_A_V2]; o.V3 = t.f[F_A_V3];
+        o.t11 = t.f[F_A_T11]; o.t22 = t.f[F_A_T22]; o.t33 = t.f[F_A_T33]; o.t12 = t.f[F_A_T12]; o.t13 = t.f[F_A_T13]; o.t23 = t.f[F_A_T23];
+        o.xg_mask = c.xg_mask;
+        for (int i = 0; i < 3; ++i) o.xg[i] = c.xg[i];
+        e.maps[a] = maps;
+        swap_state(t);
+    }
+    e.err = c.d_err;
+    e.kchunk = fused_chunk(c);
+    const int first = c.xg_mask ? 1 : 0;
+    e.nbc = (int)c.bc_run.size() - first;
+    for (int i = 0; i < e.nbc; ++i) e.bc[i] = c.bc_run[first + i];
+    return SPH_OK;
+}
+
+template <int G>
+int batch_outer_step(BatchSolve& b, BatchSweep& e) {
+    Ctx& c = *b.c;
+    const sph_solve_opts& o = *b.o;
+    double out[7];
+    int rc = outer_residual<G>(c, out);
+    if (rc) return rc;
+    b.err = out[6];
+    b.info->outer = b.outer;
+    b.info->residual = b.err;
+    if (!(b.err == b.err) || std::isinf(b.err)) { b.status = SPH_ERR_DIVERGED; b.st = BatchSolve::DONE; return SPH_OK; }
+    if (b.err < o.tol) { b.status = SPH_OK; b.st = BatchSolve::DONE; return SPH_OK; }
+    if (b.outer == o.max_outer || b.iters >= o.maxiter) { b.st = BatchSolve::DONE; return SPH_OK; }
+    if ((rc = prepare_correction<G>(c, out))) return rc;
+    b.inner = 0;
+    b.st = BatchSolve::INNER;
+    return batch_entry(c, e);
+}
+
+// end of a solve's correction phase: the bounded-wait flag, then the FP64 update
+int batch_end_inner(BatchSolve& b) {
+    Ctx& c = *b.c;
+    int rc = check_kernel_flag(c);
+    if (rc) return rc;
+    if (b.status == SPH_ERR_DIVERGED) { b.st = BatchSolve::DONE; return SPH_OK; }
+    if ((rc = apply_correction(c))) return rc;
+    ++b.outer;
+    b.st = BatchSolve::OUTER;
+    return SPH_OK;
+}
+
+// the final copies of solve_mixed_g and the solve's record
+int batch_finish(BatchSolve& b) {
+    Ctx& c = *b.c;
+    State<double>& s = c.s64;
+    const long long vol = c.d.vol;
+    if (c.prm.bc == SPH_BC_STRESS) CK(cudaMemcpyAsync(s.f[F_P], s.f[F_PRES], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
+    const int q[6] = {F_Q11, F_Q22, F_Q33, F_Q12, F_Q13, F_Q23};
+    const int d[6] = {F_T11, F_T22, F_T33, F_T12, F_T13, F_T23};
+    for (int i = 0; i < 6; ++i) CK(cudaMemcpyAsync(s.f[d[i]], s.f[q[i]], sizeof(double) * vol, cudaMemcpyDeviceToDevice, c.stream));
+    c.stale32 = true;
+    c.stale64 = false;
+    b.info->iters = b.iters;
+    b.info->err = b.err;
+    b.info->status = b.status;
+    return SPH_OK;
+}
+
+int batch_run_partial(Ctx& c, int n) {
+    switch (c.prm.geometry) {
+        case SPH_GEOM_SPHERICAL: return run_correction_sweeps<SPH>(c, n);
+        case SPH_GEOM_CYLINDRICAL: return run_correction_sweeps<CYL>(c, n);
+        default: return run_correction_sweeps<CART>(c, n);
+    }
+}
+
+int batch_outer(BatchSolve& b, BatchSweep& e) {
+    switch (b.c->prm.geometry) {
+        case SPH_GEOM_SPHERICAL: return batch_outer_step<SPH>(b, e);
+        case SPH_GEOM_CYLINDRICAL: return batch_outer_step<CYL>(b, e);
+        default: return batch_outer_step<CART>(b, e);
+    }
+}
+
+// device buffers of one lockstep batch (freed on every return path)
+struct BatchDev {
+    BatchSweep* entries = nullptr;
+    int* active = nullptr;
+    unsigned long long* red = nullptr;
+    int4* items = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    ~BatchDev() {
+        if (stream) cudaStreamSynchronize(stream);
+        if (graph) cudaGraphExecDestroy(graph);
+        if (entries) cudaFree(entries);
+        if (active) cudaFree(active);
+        if (red) cudaFree(red);
+        if (items) cudaFree(items);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+int batch_lockstep(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph_solve_info* infos) {
+    const auto t0 = std::chrono::steady_clock::now();
+    std::vector<BatchSolve> bs((size_t)n);
+    for (int32_t i = 0; i < n; ++i) {
+        BatchSolve& b = bs[i];
+        b.c = static_cast<Ctx*>(ctxs[i]);
+        b.o = &opts[i];
+        b.info = &infos[i];
+        std::memset(b.info, 0, sizeof(*b.info));
+        b.c->sweep_ms = b.c->outer_ms = 0.0;
+        b.c->hist_ms.clear();
+        b.c->corr_ready = false;
+        CK(cudaStreamSynchronize(b.c->stream));
+    }
+    const int nout = batch_nout(opts[0]);
+    BatchDev dev;
+    struct Restore {  // every context back on its own stream, on every return path
+        std::vector<BatchSolve>& bs;
+        ~Restore() { for (BatchSolve& b : bs) if (b.own) b.c->stream = b.own; }
+    } restore{bs};
+    CK(cudaStreamCreateWithFlags(&dev.stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&dev.e0));
+    CK(cudaEventCreate(&dev.e1));
+    for (BatchSolve& b : bs) { b.own = b.c->stream; b.c->stream = dev.stream; }
+    CK(cudaEventRecord(dev.e0, dev.stream));
+    for (BatchSolve& b : bs) { int rc = sync64(*b.c); if (rc) return rc; }
+
+    // work lists: blocks of every solve's fused sweep, BC stages and inner test, per geometry
+    std::vector<BatchSweep> host((size_t)n);
+    std::vector<int4> items;
+    size_t fz_off[3], fz_n[3], nm_off[3], nm_n[3], bc_off[3][kBatchMaxBc], bc_n[3][kBatchMaxBc];
+    for (int g = 0; g < 3; ++g) {
+        fz_off[g] = items.size();
+        for (int32_t i = 0; i < n; ++i) {
+            Ctx& c = *bs[i].c;
+            if (c.prm.geometry != g) continue;
+            const int kc = fused_chunk(c);
+            const int gx = (c.d.n1 + FTX - 1) / FTX, gy = (c.d.n2 + FTY - 1) / FTY, gz = (c.d.n3 + kc - 1) / kc;
+            for (int z = 0; z < gz; ++z) for (int y = 0; y < gy; ++y) for (int x = 0; x < gx; ++x) items.push_back(make_int4(i, x, y, z));
+        }
+        fz_n[g] = items.size() - fz_off[g];
+        for (int t = 0; t < kBatchMaxBc; ++t) {
+            bc_off[g][t] = items.size();
+            for (int32_t i = 0; i < n; ++i) {
+                Ctx& c = *bs[i].c;
+                const int first = c.xg_mask ? 1 : 0;
+                if (c.prm.geometry != g || first + t >= (int)c.bc_run.size()) continue;
+                const BcStage& st = c.bc_run[first + t];
+                const int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1, ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
+                for (int v = 0; v < (ev + 7) / 8; ++v) for (int u = 0; u < (eu + 31) / 32; ++u) items.push_back(make_int4(i, u, v, 0));
+            }
+            bc_n[g][t] = items.size() - bc_off[g][t];
+        }
+        nm_off[g] = items.size();
+        for (int32_t i = 0; i < n; ++i) {
+            Ctx& c = *bs[i].c;
+            if (c.prm.geometry != g) continue;
+            const dim3 gv = grid_vel(c.d);
+            for (unsigned z = 0; z < gv.z; ++z) for (unsigned y = 0; y < gv.y; ++y) for (unsigned x = 0; x < gv.x; ++x)
+                items.push_back(make_int4(i, (int)x, (int)y, (int)z));
+        }
+        nm_n[g] = items.size() - nm_off[g];
+    }
+    if (cudaMalloc((void**)&dev.entries, sizeof(BatchSweep) * n) != cudaSuccess || cudaMalloc((void**)&dev.active, sizeof(int) * n) != cudaSuccess ||
+        cudaMalloc((void**)&dev.red, sizeof(unsigned long long) * n) != cudaSuccess ||
+        cudaMalloc((void**)&dev.items, sizeof(int4) * std::max<size_t>(items.size(), 1)) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SPH_ERR_NOMEM, "batched solve: device work lists");
+    }
+    CK(cudaMemcpyAsync(dev.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, dev.stream));
+    CK(cudaMemsetAsync(dev.entries, 0, sizeof(BatchSweep) * n, dev.stream));
+    std::vector<int> act((size_t)n, 0);
+
+    // one round: nout sweeps of every active solve (arrangement a = s & 1 read by sweep s)
+    auto capture = [&]() -> int {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(dev.stream, cudaStreamCaptureModeThreadLocal));
+        for (int sw = 0; sw < nout; ++sw) {
+            const int a = sw & 1;
+            if (fz_n[SPH]) k_fused_tma_batch<SPH><<<(unsigned)fz_n[SPH], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[SPH], dev.active, a);
+            if (fz_n[CYL]) k_fused_tma_batch<CYL><<<(unsigned)fz_n[CYL], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[CYL], dev.active, a);
+            if (fz_n[CART]) k_fused_tma_batch<CART><<<(unsigned)fz_n[CART], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[CART], dev.active, a);
+            for (int t = 0; t < kBatchMaxBc; ++t) {
+                if (bc_n[SPH][t]) k_bc_batch<SPH><<<(unsigned)bc_n[SPH][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[SPH][t], dev.active, a, t);
+                if (bc_n[CYL][t]) k_bc_batch<CYL><<<(unsigned)bc_n[CYL][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[CYL][t], dev.active, a, t);
+                if (bc_n[CART][t]) k_bc_batch<CART><<<(unsigned)bc_n[CART][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[CART][t], dev.active, a, t);
+            }
+        }
+        cudaError_t e = cudaStreamEndCapture(dev.stream, &g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("batch graph capture: ") + cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&dev.graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SPH_ERR_CUDA, std::string("batch graph instantiate: ") + cudaGetErrorString(e));
+        return SPH_OK;
+    };
+
+    for (;;) {
+        int rc;
+        // FP64 outer steps of the solves between correction phases
+        for (int32_t i = 0; i < n; ++i)
+            if (bs[i].st == BatchSolve::OUTER) {
+                if ((rc = batch_outer(bs[i], host[i]))) return rc;
+                if (bs[i].st == BatchSolve::INNER)
+                    CK(cudaMemcpyAsync(dev.entries + i, &host[i], sizeof(BatchSweep), cudaMemcpyHostToDevice, dev.stream));
+            }
+        // the next chunk of every solve in its correction phase: full chunks go into the round
+        bool any = false, pending = false;
+        for (int32_t i = 0; i < n; ++i) {
+            BatchSolve& b = bs[i];
+            act[i] = 0;
+            if (b.st != BatchSolve::INNER) continue;
+            const int64_t inner_max = b.o->inner_max > 0 ? b.o->inner_max : 100000;
+            const int64_t chunk = std::min<int64_t>(std::min<int64_t>(nout, inner_max - b.inner), b.o->maxiter - b.iters);
+            if (chunk <= 0) {  // the inner loop's condition fails before a sweep
+                if ((rc = batch_end_inner(b))) return rc;
+            } else if (chunk < nout) {  // a last, shorter chunk: this solve alone, no inner test after it
+                if ((rc = batch_run_partial(*b.c, (int)chunk))) return rc;
+                b.inner += chunk;
+                b.iters += chunk;
+                if ((rc = batch_end_inner(b))) return rc;
+            } else {
+                act[i] = 1;
+                any = true;
+            }
+        }
+        for (const BatchSolve& b : bs) pending |= b.st != BatchSolve::DONE;
+        if (!any) {
+            if (!pending) break;
+            continue;
+        }
+        if (!dev.graph && (rc = capture())) return rc;
+        CK(cudaMemcpyAsync(dev.active, act.data(), sizeof(int) * n, cudaMemcpyHostToDevice, dev.stream));
+        CK(cudaGraphLaunch(dev.graph, dev.stream));
+        CK(cudaMemsetAsync(dev.red, 0, sizeof(unsigned long long) * n, dev.stream));
+        if (nm_n[SPH]) k_velocity_norm_batch<SPH><<<(unsigned)nm_n[SPH], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + nm_off[SPH], dev.active, dev.red);
+        if (nm_n[CYL]) k_velocity_norm_batch<CYL><<<(unsigned)nm_n[CYL], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + nm_off[CYL], dev.active, dev.red);
+        if (nm_n[CART]) k_velocity_norm_batch<CART><<<(unsigned)nm_n[CART], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + nm_off[CART], dev.active, dev.red);
+        CK(cudaGetLastError());
+        std::vector<unsigned long long> red((size_t)n);
+        CK(cudaMemcpyAsync(red.data(), dev.red, sizeof(unsigned long long) * n, cudaMemcpyDeviceToHost, dev.stream));
+        CK(cudaStreamSynchronize(dev.stream));
+        for (int32_t i = 0; i < n; ++i) {
+            if (!act[i]) continue;
+            BatchSolve& b = bs[i];
+            b.inner += nout;
+            b.iters += nout;
+            double ri;
+            std::memcpy(&ri, &red[i], sizeof(double));
+            bool end = false;
+            if (!(ri == ri) || std::isinf(ri)) { b.status = SPH_ERR_DIVERGED; end = true; }
+            else if (ri <= b.o->inner_rtol * b.c->corr_r0) end = true;
+            if (end && (rc = batch_end_inner(b))) return rc;
+        }
+    }
+    for (BatchSolve& b : bs) { int rc = batch_finish(b); if (rc) return rc; }
+    CK(cudaEventRecord(dev.e1, dev.stream));
+    CK(cudaEventSynchronize(dev.e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, dev.e0, dev.e1));
+    const double wall = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (BatchSolve& b : bs) { b.info->seconds = wall; b.info->device_ms = ms; b.c->last_ms = ms; }
+    return SPH_OK;
+}
+
+// ---------------------------------------------------------------------------
 int check_params(const sph_params* p) {
     if (!p) return fail(SPH_ERR_INVALID, "params is NULL");
     if (p->abi_version != SPH_ABI_VERSION) return fail(SPH_ERR_INVALID, "abi_version mismatch");
@@ -1422,6 +1730,13 @@ int sph_batch_solve(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sp
             if (ctxs[j] == ctxs[i]) return fail(SPH_ERR_INVALID, "sph_batch_solve: a context appears twice");
     }
     if (n == 0) return SPH_OK;
+    // lockstep batch: every solve mixed-precision on the FP64 residual, no warm start, the TMA
+    // sweep, one nout for all (the common case of a parameter sweep); else one host thread per
+    // solve at a time, each on its own stream
+    bool lockstep = true;
+    for (int32_t i = 0; i < n && lockstep; ++i)
+        lockstep = batch_eligible(*static_cast<Ctx*>(ctxs[i]), opts[i]) && batch_nout(opts[i]) == batch_nout(opts[0]);
+    if (lockstep) return batch_lockstep(ctxs, n, opts, infos);
     int nt = threads > 0 ? threads : (int)std::thread::hardware_concurrency();
     nt = std::max(1, std::min(nt, (int)n));
     int dev = 0;

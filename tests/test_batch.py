@@ -82,3 +82,58 @@ def test_batch_rejects_a_context_twice():
     with S.Solver(_small_cases("fp64")[3]) as sv:
         with pytest.raises(S.SphError):
             S.solve_batch([sv, sv], S.make_opts(maxiter=10), threads=2)
+
+
+def _lockstep_cases():
+    """uneven grids of all three geometries, linear and power law, mixed precision"""
+    return [
+        S.sector_params((23, 17, 15), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
+                        sig_bc=(0.0, 0.5, -0.5), incl_linear=1, precision="mixed"),
+        S.default_params("cylindrical", n1=19, n2=15, n3=13, rheology="linear", bc="stress", sig_bc=(0.0, 0.3, -0.3),
+                         incl_linear=1, precision="mixed"),
+        S.default_params("cartesian", n1=33, n2=15, n3=19, rheology="linear", incl_linear=1, precision="mixed"),
+        S.sector_params((31, 15, 21), bc="free_slip", rheology="linear", precision="mixed"),
+        S.sector_params((15, 41, 9), bc="diapir", rheology="linear", precision="mixed"),
+    ]
+
+
+@pytest.mark.gpu
+def test_lockstep_batch_equals_serial_with_own_budgets_and_a_diverging_solve():
+    """The lockstep batch (one launch per sweep over all solves' blocks, rounds replayed from a
+    graph): per-solve budgets that end inside a round (a last, shorter chunk), a solve stopped by
+    max_outer, and a solve whose state holds a NaN (diverges at its first check) — every solve's
+    status, iteration count and fields equal those of the same solve alone."""
+    budgets = [(20000, 4000, 30), (1250, 600, 30), (20000, 4000, 1), (777, 300, 30), (20000, 4000, 30)]
+    opts = [S.make_opts(tol=1e-8, maxiter=m, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=mo, inner_max=im)
+            for m, im, mo in budgets]
+
+    def plant(sv, i):
+        if i == 4:
+            v = sv.get("V2")
+            v[5, 20, 4] = np.nan
+            sv.set("V2", v)
+
+    serial, fields_s = [], []
+    for i, (p, o) in enumerate(zip(_lockstep_cases(), opts)):
+        with S.Solver(p) as sv:
+            plant(sv, i)
+            serial.append(sv.solve(tol=o.tol, maxiter=o.maxiter, nout=o.nout, criterion="residual", inner_rtol=o.inner_rtol,
+                                   max_outer=o.max_outer, inner_max=o.inner_max))
+            fields_s.append({f: sv.get(f) for f in FIELDS})
+    solvers = [S.Solver(p) for p in _lockstep_cases()]
+    try:
+        for i, sv in enumerate(solvers):
+            plant(sv, i)
+        res = S.solve_batch(solvers, opts)
+        fields_b = [{f: sv.get(f) for f in FIELDS} for sv in solvers]
+    finally:
+        for sv in solvers:
+            sv.close()
+    assert len({r.seconds for r in res}) == 1  # one lockstep batch: the batch's wall time for every solve
+    assert serial[4].status == S.SPH_ERR_DIVERGED and serial[2].outer == 1 and serial[1].iters == 1250
+    for i, (a, b) in enumerate(zip(serial, res)):
+        assert (a.status, a.iters, a.outer) == (b.status, b.iters, b.outer), i
+        if a.status != S.SPH_ERR_DIVERGED:
+            assert a.residual == b.residual, i
+            for f in FIELDS:
+                np.testing.assert_array_equal(fields_b[i][f], fields_s[i][f], err_msg=f"case {i} {f}")

@@ -62,8 +62,12 @@ typedef enum sph_bc {
     SPH_BC_DIAPIR = 0,     /* simple shear of the diapir scripts (sph: SphericalStokes_diapir.jl:61-99,
                               cyl: CylindricalStokes_diapir.jl:358-366, cart: CartesianStokes_diapir.jl:371-379) */
     SPH_BC_FREE_SLIP = 1,  /* free slip on all faces (SphericalStokes_plateau.jl:64-92); spherical only */
-    SPH_BC_STRESS = 2      /* free slip on the x1 faces, prescribed total normal stress sig_bc[1] on the x2
+    SPH_BC_STRESS = 2,     /* free slip on the x1 faces, prescribed total normal stress sig_bc[1] on the x2
                               faces and sig_bc[2] on the x3 faces (not in the reference); spherical only */
+    SPH_BC_FREE_SURFACE = 3 /* free-surface-stabilised top (not in the reference; the plateau's topography load
+                              without sticky air): on the top x1 face the traction of the surface load q
+                              (field SPH_FIELD_TOP_LOAD, top cells) plus fs_kappa * V_r, zero shear traction;
+                              free slip on the bottom and the x2, x3 faces; spherical only */
 } sph_bc;
 
 /* rheology update after the stress update */
@@ -114,7 +118,9 @@ typedef enum sph_field {
     SPH_FIELD_RHO = 15,
     SPH_FIELD_PHASE = 16,  /* 1 = linear cell for the power laws, 0 = power law (values 0/1 as double) */
     SPH_FIELD_ETA_PL = 17, /* η_PL state of SPH_RHEO_TAU_POWER_RELAX */
-    SPH_FIELD_COUNT = 18
+    SPH_FIELD_TOP_LOAD = 18, /* SPH_BC_FREE_SURFACE: surface load q (normal stress of the topography's weight)
+                                on the top cells (i = n1); a cell-size array, the other layers unused */
+    SPH_FIELD_COUNT = 19
 } sph_field;
 
 /* grid, physics and PT parameters.  sph_params_default() fills the values of
@@ -150,7 +156,9 @@ typedef struct sph_params {
     int32_t kernels;       /* sph_kernels: FP32 sweeps fused (default) or one kernel per reference step */
     int32_t etasm_passes;  /* passes of the 7-point max filter that gives ηSM (reference: 1; 0 means 1) */
     int32_t reserved_i;
-    double reserved[8];
+    double fs_kappa;       /* SPH_BC_FREE_SURFACE: stabilisation coefficient θ Δt Δρ g of the free-surface
+                              stabilisation algorithm (the load of the surface's rise over a step; 0: none) */
+    double reserved[7];
 } sph_params;
 
 /* solve controls and result */

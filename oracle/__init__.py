@@ -33,7 +33,7 @@ class SphState(C.Structure):
 class SphParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("_dr", "_dt", "_dp", "dmp", "vpdt", "lr", "g", "tau_C", "n_exp", "r", "sh")] + [
         ("bc", C.c_int32), ("rheo", C.c_int32)] + [(n, C.c_double) for n in ("relax", "edot_bg", "sig_t", "sig_p")] + [
-        ("passes", C.c_int32), ("pad_", C.c_int32)]
+        ("passes", C.c_int32), ("pad_", C.c_int32), ("fs_kappa", C.c_double), ("top_load", _PD)]
 
 
 _lib = None
@@ -85,10 +85,10 @@ class Sph:
 
     NAMES = {"P": "P", "V1": "VR", "V2": "Vt", "V3": "Vp", "TAU11": "tRR", "TAU22": "ttt", "TAU33": "tpp",
              "TAU12": "tRt", "TAU13": "tRp", "TAU23": "ttp", "ETA": "eta", "ETA_INI": "eta_ini", "ETA_SM": "etaSM",
-             "DT_R": "DT_R", "TII": "tII", "RHO": "rho"}
+             "DT_R": "DT_R", "TII": "tII", "RHO": "rho", "TOP_LOAD": "top_load"}
 
     def __init__(self, nr, nt, np_, *, r, c2, lr, lt, lp, l_ref, dmp, vpdt, g, tau_C, n_exp, sh, bc, rheo,
-                 relax=0.5, edot_bg=1.0, sig_t=0.0, sig_p=0.0, c1=None, c3=0.0, passes=1):
+                 relax=0.5, edot_bg=1.0, sig_t=0.0, sig_p=0.0, c1=None, c3=0.0, passes=1, fs_kappa=0.0):
         self.n = (nr, nt, np_)
         c1 = r if c1 is None else c1
         z = lambda *s: np.zeros(s, dtype=np.float64, order="F")
@@ -107,7 +107,8 @@ class Sph:
         self.eta_tmp = np.zeros(nr * nt * np_ + int(lib().orc_sph_scratch_size(nr, nt, np_)), dtype=np.float64)
         self.prm = SphParams(_dr=(nr - 1) / lr, _dt=(nt - 1) / lt, _dp=(np_ - 1) / lp, dmp=dmp, vpdt=vpdt, lr=l_ref,
                              g=g, tau_C=tau_C, n_exp=n_exp, r=r, sh=sh, bc=bc, rheo=rheo, relax=relax,
-                             edot_bg=edot_bg, sig_t=sig_t, sig_p=sig_p, passes=passes)
+                             edot_bg=edot_bg, sig_t=sig_t, sig_p=sig_p, passes=passes, fs_kappa=fs_kappa)
+        self.top_load = np.zeros((nr, nt, np_), dtype=np.float64, order="F")  # free-surface load (top layer read)
         self._sync()
 
     def _sync(self):
@@ -117,6 +118,7 @@ class Sph:
         s.phase = self.phase.ctypes.data_as(_PU8)
         s.eta_tmp = _ptr(self.eta_tmp)
         self.st = s
+        self.prm.top_load = _ptr(self.top_load)
 
     @classmethod
     def from_params(cls, p) -> "Sph":
@@ -125,7 +127,8 @@ class Sph:
         o = cls(p.n1, p.n2, p.n3, r=p.r, c1=p.c1, c2=p.c2, c3=p.c3, lr=p.l1, lt=p.l2, lp=p.l3, l_ref=p.l_ref,
                 dmp=p.dmp, vpdt=p.vpdt if p.vpdt > 0 else p.l1 / (p.n1 - 1) / (2.0 + 4.5 * math.log10(p.vr)),
                 g=p.g, tau_C=p.tau_C, n_exp=p.n_exp, sh=p.sh, bc=p.bc, rheo=rheo, relax=p.relax,
-                edot_bg=p.edot_bg, sig_t=p.sig_bc[1], sig_p=p.sig_bc[2], passes=max(1, p.etasm_passes))
+                edot_bg=p.edot_bg, sig_t=p.sig_bc[1], sig_p=p.sig_bc[2], passes=max(1, p.etasm_passes),
+                fs_kappa=getattr(p, "fs_kappa", 0.0))
         o.rho[:] = p.rho0
         o.eta[:] = p.eta0
         if p.init == 1:
@@ -185,6 +188,10 @@ class Sph:
             L = lib()
             L.orc_sph_stress_pressure.argtypes = [_PD, _PD, _PD, C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double]
             L.orc_sph_stress_pressure(_ptr(self.P), _ptr(self.ttt), _ptr(self.tpp), *self.n, self.prm.sig_t, self.prm.sig_p)
+        if self.prm.bc == 3:
+            L = lib()
+            L.orc_sph_fs_pressure.argtypes = [_PD] * 4 + [C.c_int64] * 3 + [C.c_double]
+            L.orc_sph_fs_pressure(_ptr(self.P), _ptr(self.tRR), _ptr(self.VR), _ptr(self.top_load), *self.n, self.prm.fs_kappa)
 
     def power_law(self):
         nr, nt, np_ = self.n

@@ -78,6 +78,8 @@ struct orc_sph_params {
     double sig_t, sig_p;   // EXT far-field normal stresses on the theta / phi faces
     int32_t passes;        // EXT applications of the 7-point max filter giving ηSM (reference: 1)
     int32_t pad_;
+    double fs_kappa;          // EXT bc 3: stabilisation coefficient of the free surface (θ Δt Δρ g)
+    const double* top_load;   // EXT bc 3: surface load q per top cell (cell layout, top layer read; NULL: 0)
 };
 
 static inline Arr A(double* p, long n1, long n2, long n3) { return Arr{p, n1, n2, n3}; }
@@ -431,10 +433,50 @@ void orc_sph_stress_pressure(double* Pa, const double* ttt, const double* tpp, i
             }
 }
 
+// EXT free-surface top boundary (bc 3, the plateau's topography load without sticky air): the
+// top radial face carries the traction of a surface load q(θ,φ) plus the stabilisation term
+// κ V_r of the free-surface stabilisation algorithm (the load of the surface's rise over a time
+// step, κ = θ Δt Δρ g), with zero shear traction; the bottom face and the θ, φ faces are free
+// slip.  As for the far-field stress BC, the boundary passes through the top cells' centres:
+// the ghost VR(nr+1) makes the top cell divergence-free and the top cell's pressure is slaved
+// to the traction (orc_sph_fs_pressure).  BC_R's copies of Vθ, Vφ come first, the ghost uses them.
+static void sph_bc_R_fs(orc_sph_state* s, const orc_sph_params* q) {
+    const long nr = s->nr, nt = s->nt, np = s->np;
+    Arr VR = A(s->VR, nr + 1, nt, np), Vt = A(s->Vt, nr, nt + 1, np), Vp = A(s->Vp, nr, nt, np + 1);
+    Arr R = A(s->R, nr, nt, np), th = A(s->th, nr, nt, np);
+    for (long k = 1; k <= np; ++k) for (long j = 1; j <= nt; ++j) VR(1, j, k) = -VR(2, j, k);
+    for (long k = 1; k <= np; ++k) for (long j = 1; j <= nt + 1; ++j) { Vt(1, j, k) = Vt(2, j, k); Vt(nr, j, k) = Vt(nr - 1, j, k); }
+    for (long k = 1; k <= np + 1; ++k) for (long j = 1; j <= nt; ++j) { Vp(1, j, k) = Vp(2, j, k); Vp(nr, j, k) = Vp(nr - 1, j, k); }
+    const double _dr = q->_dr, _dt = q->_dt, _dp = q->_dp;
+    for (long k = 1; k <= np; ++k)
+        for (long j = 1; j <= nt; ++j) {
+            double Rc = R(nr, j, k), tc = th(nr, j, k);
+            double a2 = _dt / Rc, a3 = _dp / (Rc * std::sin(tc)), c1 = 2.0 / Rc, c2 = cot(tc) / Rc;
+            double v = VR(nr, j, k);
+            double avy = 0.5 * (Vt(nr, j, k) + Vt(nr, j + 1, k));
+            // DIVV of cell nr = A0 + B * ghost = 0
+            double A0 = -_dr * v + 0.5 * c1 * v + a2 * (Vt(nr, j + 1, k) - Vt(nr, j, k)) + a3 * (Vp(nr, j, k + 1) - Vp(nr, j, k)) + c2 * avy;
+            double B = _dr + 0.5 * c1;
+            VR(nr + 1, j, k) = -A0 / B;
+        }
+}
+
+// EXT: top-cell pressure of the free-surface BC, P = τ_RR + q + κ V_r (V_r at the cell centre:
+// the mean of the top cell's inner face and ghost); load NULL: q = 0
+void orc_sph_fs_pressure(double* Pa, const double* tRR, const double* VRa, const double* load, int64_t nr, int64_t nt, int64_t np,
+                         double kappa) {
+    Arr P = A(Pa, nr, nt, np), T1 = A(const_cast<double*>(tRR), nr, nt, np), VR = A(const_cast<double*>(VRa), nr + 1, nt, np);
+    Arr L = A(const_cast<double*>(load), nr, nt, np);
+    for (long k = 1; k <= np; ++k)
+        for (long j = 1; j <= nt; ++j)
+            P(nr, j, k) = T1(nr, j, k) + (load ? L(nr, j, k) : 0.0) + kappa * 0.5 * (VR(nr, j, k) + VR(nr + 1, j, k));
+}
+
 void orc_sph_apply_bc(orc_sph_state* s, const orc_sph_params* q) {
-    sph_bc_R(s);
+    if (q->bc == 3) sph_bc_R_fs(s, q);
+    else sph_bc_R(s);
     if (q->bc == 0) { sph_bc_t_diapir(s, q); sph_bc_p_diapir(s, q); }
-    else if (q->bc == 1) { sph_bc_t_free(s); sph_bc_p_free(s); }
+    else if (q->bc == 1 || q->bc == 3) { sph_bc_t_free(s); sph_bc_p_free(s); }
     else { sph_bc_t_free(s, false); sph_bc_stress_t(s, q); sph_bc_p_free(s, false); sph_bc_stress_p(s, q); }
 }
 
@@ -542,6 +584,7 @@ void orc_sph_iterate(orc_sph_state* s, const orc_sph_params* q, int64_t niter) {
         }
         orc_sph_compute_P(s, q);
         if (q->bc == 2) orc_sph_stress_pressure(s->P, s->ttt, s->tpp, nr, nt, np, q->sig_t, q->sig_p);
+        if (q->bc == 3) orc_sph_fs_pressure(s->P, s->tRR, s->VR, q->top_load, nr, nt, np, q->fs_kappa);
         if (q->rheo == 0) {
             orc_sph_compute_TII(s);
             orc_copy_BC(s->tII, nr, nt, np);
@@ -667,6 +710,11 @@ void orc_sph_residual(orc_sph_state* s, const orc_sph_params* q, double* out, do
         orc_sph_stress_pressure(Pres.data(), ttt, tpp, nr, nt, np, q->sig_t, q->sig_p);
         t.P = Pres.data();
     }
+    if (q->bc == 3) {  // top-cell pressure of the free surface from the viscous stress
+        Pres.assign(s->P, s->P + nc);
+        orc_sph_fs_pressure(Pres.data(), tRR, s->VR, q->top_load, nr, nt, np, q->fs_kappa);
+        t.P = Pres.data();
+    }
     long nv[3] = {(nr + 1) * nt * np, nr * (nt + 1) * np, nr * nt * (np + 1)};
     double* own[3] = {rVR, rVt, rVp};
     double* tmp[3];
@@ -713,6 +761,7 @@ void orc_sph_corr_sweep(orc_sph_state* s, const orc_sph_params* q, const double*
     for (int64_t it = 0; it < nsweeps; ++it) {
         sph_compute_P_impl(s, &h, rP);
         if (h.bc == 2) orc_sph_stress_pressure(s->P, s->ttt, s->tpp, s->nr, s->nt, s->np, 0.0, 0.0);
+        if (h.bc == 3) orc_sph_fs_pressure(s->P, s->tRR, s->VR, nullptr, s->nr, s->nt, s->np, h.fs_kappa);
         sph_compute_V_impl(s, &h, rV);
         orc_sph_apply_bc(s, &h);
     }

@@ -29,7 +29,7 @@ SPH_OK, SPH_ERR_INVALID, SPH_ERR_CUDA, SPH_ERR_NOT_CONVERGED, SPH_ERR_DIVERGED =
 SPH_ERR_NOMEM, SPH_ERR_UNSUPPORTED, SPH_ERR_NO_DEVICE = -5, -6, -7
 GEOM = {"spherical": 0, "cylindrical": 1, "cartesian": 2}
 PREC = {"fp64": 0, "fp32": 1, "mixed": 2}
-BC = {"diapir": 0, "free_slip": 1, "stress": 2}
+BC = {"diapir": 0, "free_slip": 1, "stress": 2, "free_surface": 3}
 RHEO = {"linear": 0, "tau_power": 1, "tau_power_relax": 2, "edot_power_relax": 3}
 INIT = {"none": 0, "inclusion": 1}
 KERNELS_VARIANT = {"auto": 0, "simple": 1}
@@ -37,7 +37,7 @@ CRIT = {"reference": 0, "residual": 1, "reference_plateau": 2}
 FIELDS = {
     "P": 0, "V1": 1, "V2": 2, "V3": 3, "TAU11": 4, "TAU22": 5, "TAU33": 6,
     "TAU12": 7, "TAU13": 8, "TAU23": 9, "ETA": 10, "ETA_INI": 11, "ETA_SM": 12,
-    "DT_R": 13, "TII": 14, "RHO": 15, "PHASE": 16, "ETA_PL": 17,
+    "DT_R": 13, "TII": 14, "RHO": 15, "PHASE": 16, "ETA_PL": 17, "TOP_LOAD": 18,
 }
 # the reference's array names (SphericalStokes_diapir.jl:381-399) -> field ids
 ALIASES = {
@@ -74,7 +74,7 @@ class Params(C.Structure):
         ("eta0", C.c_double), ("vr", C.c_double), ("rho0", C.c_double), ("rho_in", C.c_double),
         ("radius", C.c_double), ("incl_linear", C.c_int32), ("kernels", C.c_int32),
         ("etasm_passes", C.c_int32), ("reserved_i", C.c_int32),
-        ("reserved", C.c_double * 8),
+        ("fs_kappa", C.c_double), ("reserved", C.c_double * 7),
     ]
 
 

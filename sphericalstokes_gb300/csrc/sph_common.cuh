@@ -65,6 +65,9 @@ struct KP {
     T tau_C, n_exp, relax, edot_bg;
     T sig2, sig3;                      // prescribed total normal stress on x2 / x3 faces
     int traction;                      // 1: boundary cells on x2/x3 faces take P = τ_nn - σ_bc
+    int fs;                            // 1: top cells (i = n1-1) take the free-surface pressure (fs_pressure)
+    T fs_kappa;                        // free-surface stabilisation coefficient
+    const T* top_load;                 // surface load per top cell (NULL: 0, the homogeneous problem)
     unsigned long long* red;           // reduction slots (max of |x| as ordered bits)
 };
 
@@ -91,6 +94,14 @@ __device__ __forceinline__ bool traction_pressure(int j, int k, int n2, int n3, 
     if (b2 && b3) P = ((t22 - sig2) + (t33 - sig3)) / T(2);
     else P = b2 ? (t22 - sig2) : (t33 - sig3);
     return true;
+}
+
+// pressure of a top cell under the free-surface BC: the normal traction balances the surface
+// load q and the stabilisation term, -P + τ11 = -(q + κ V_r), V_r at the cell centre = the mean
+// of the cell's inner radial face v_in and its ghost v_out
+template <typename T>
+__device__ __forceinline__ T fs_pressure(T t11, T q, T kappa, T v_in, T v_out) {
+    return t11 + q + kappa * (T(0.5) * (v_in + v_out));
 }
 
 // Order-preserving bits of |x|: for non-negative doubles the unsigned order of the

@@ -166,6 +166,8 @@ __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o
                 v22 = (O[I22][b][a] + 2.f * gs * D.D22) * f;
                 v33 = (O[I33][b][a] + 2.f * gs * D.D33) * f;
                 if (p.traction) traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
+                if (p.fs && x == n1 - 1)
+                    vP = fs_pressure(v11, p.top_load ? p.top_load[g] : 0.f, p.fs_kappa, I0[0][b][a], I0[0][b][a + 1]);
                 vdt = pdiv(vpdt2, kb + gs * f);
                 if (own) { o.P[g] = vP; o.t11[g] = v11; o.t22[g] = v22; o.t33[g] = v33; }
             }
@@ -528,6 +530,7 @@ __device__ __forceinline__ void fused_tma_body(const KP<float>& p, const FusedOu
     const CellMetric<float> cm = cell_metric_t<float, G>(p.geo, d2, d3, clampi(x, 0, n1 - 1), clampi(y, 0, n2 - 1));
     const int gxy = x + d.sy * y;
     const bool y_face = y == 0 || y == n2 - 1;  // stage-1 point on an x2 face of the box
+    const bool fs_top = p.fs && x == n1 - 1;    // stage-1 point in a free-surface top cell
     const int iin = b * TIN_X + a + 3;   // input-tile index of the stage-1 point
     const int iold = b * TOLD_X + a + 3; // old-tile index of the stage-1 point
     const int tx = lane, ty = warp;      // velocity node (warps < FTY)
@@ -576,6 +579,8 @@ __device__ __forceinline__ void fused_tma_body(const KP<float>& p, const FusedOu
             } else if (p.traction) {
                 traction_pressure(y, k, n2, n3, v22, v33, p.sig2, p.sig3, vP);
             }
+            // free-surface top cell (the correction problem is homogeneous: no load)
+            if (fs_top) vP = fs_pressure(v11, MODE == 1 ? 0.f : p.top_load[g], p.fs_kappa, ov1, in0(0, 0, 1));
             vdt = pdiv(vpdt2, kb + gs * f);
         }
         {

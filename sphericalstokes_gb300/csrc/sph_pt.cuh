@@ -54,10 +54,12 @@ __global__ void __launch_bounds__(256) k_stress(KP<T> p) {
         T dv = D.div;
         if (RHS) dv += p.rP[c];
         T Pn = p.P[c] - kb * dv;
+        const T n11 = (p.t11[c] + T(2) * gs * D.D11) * f;
         const T n22 = (p.t22[c] + T(2) * gs * D.D22) * f, n33 = (p.t33[c] + T(2) * gs * D.D33) * f;
         if (p.traction) traction_pressure(j, k, d.n2, d.n3, n22, n33, p.sig2, p.sig3, Pn);
+        if (p.fs && i == d.n1 - 1) Pn = fs_pressure(n11, p.top_load ? p.top_load[c] : T(0), p.fs_kappa, p.V1[c], p.V1[c + 1]);
         p.P[c] = Pn;
-        p.t11[c] = (p.t11[c] + T(2) * gs * D.D11) * f;
+        p.t11[c] = n11;
         p.t22[c] = n22;
         p.t33[c] = n33;
         p.DT_R[c] = pdiv(p.vpdt2, kb + gs * f);
@@ -364,7 +366,7 @@ __global__ void __launch_bounds__(256) k_tau_visc(KP<T> p) {
 // into their ghost layer; it reads those fields at the copies' source cells
 // instead of at the ghosts the copies are writing (the same values)
 enum BcKind { BC_NEG = 0, BC_COPY = 1, BC_ZERO = 2, BC_LIN = 3, BC_LIN2M = 4, BC_STRESS = 5, BC_STRESS_SRC = 6 };
-struct BcOp { int field; int kind; int cd; double c0, c1; };
+struct BcOp { int field; int kind; int cd; double c0, c1; int side; };  // side: -1 both faces, 0 low, 1 high
 struct BcStage { int dim; int nops; BcOp op[3]; };
 
 template <typename T>
@@ -388,6 +390,7 @@ __device__ __forceinline__ void bc_body(const KP<T>& p, const BcStage& st, int h
         const int stride[3] = {1, sy, sz};
         const int base = u * stride[du] + v * stride[dv];
         for (int side = 0; side < 2; ++side) {
+            if (op.side >= 0 && op.side != side) continue;
             const int b = side == 0 ? 0 : ext[D] - 1;
             const int in = side == 0 ? 1 : ext[D] - 2;
             const int cb = base + b * stride[D], ci = base + in * stride[D];
@@ -410,7 +413,7 @@ __device__ __forceinline__ void bc_body(const KP<T>& p, const BcStage& st, int h
                     val = T(2) * (xc[idx] - T(op.c1)) * T(op.c0) - A[ci];
                     break;
                 }
-                default: {  // BC_STRESS: normal ghost of V2 (D == 1) or V3 (D == 2) from div V = 0 in the boundary cell
+                default: {  // BC_STRESS: normal ghost of V1 (D == 0), V2 (D == 1) or V3 (D == 2) from div V = 0 in the boundary cell
                     const int cellb = side == 0 ? 0 : ext[D] - 2;        // boundary cell index along D
                     // boundary cell (its tangential velocities: at the ghost, or at the source of its copy)
                     const int cc = base + (op.kind == BC_STRESS_SRC ? cellb + (side == 0 ? 1 : -1) : cellb) * stride[D];
@@ -421,7 +424,12 @@ __device__ __forceinline__ void bc_body(const KP<T>& p, const BcStage& st, int h
                     const T avx = (p.V1[cc] + p.V1[cc + 1]) * T(0.5);
                     const T vin = A[ci];
                     T A0, B;
-                    if (D == 1) {
+                    if (D == 0) {  // V1 ghost of the free-surface top (or bottom) face
+                        const T avy = (p.V2[cc] + p.V2[cc + sy]) * T(0.5);
+                        A0 = p.d1 * (-sgn) * vin + T(0.5) * m.c1 * vin + m.a2 * (p.V2[cc + sy] - p.V2[cc]) + m.a3 * (p.V3[cc + sz] - p.V3[cc]) +
+                             m.c2 * avy;
+                        B = p.d1 * sgn + T(0.5) * m.c1;
+                    } else if (D == 1) {
                         A0 = p.d1 * (p.V1[cc + 1] - p.V1[cc]) + m.a3 * (p.V3[cc + sz] - p.V3[cc]) + m.c1 * avx + m.a2 * (-sgn) * vin + m.c2 * T(0.5) * vin;
                         B = m.a2 * sgn + T(0.5) * m.c2;
                     } else {
@@ -454,7 +462,8 @@ __global__ void k_traction_pressure(KP<T> p, T* __restrict__ Pout) {
     if (i >= d.n1 || j >= d.n2 || k >= d.n3) return;
     const int c = i + d.sy * j + d.sz * k;
     T P = p.P[c];
-    traction_pressure(j, k, d.n2, d.n3, p.t22[c], p.t33[c], p.sig2, p.sig3, P);
+    if (p.traction) traction_pressure(j, k, d.n2, d.n3, p.t22[c], p.t33[c], p.sig2, p.sig3, P);
+    if (p.fs && i == d.n1 - 1) P = fs_pressure(p.t11[c], p.top_load ? p.top_load[c] : T(0), p.fs_kappa, p.V1[c], p.V1[c + 1]);
     Pout[c] = P;
 }
 

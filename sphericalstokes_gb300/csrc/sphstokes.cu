@@ -64,6 +64,7 @@ enum FieldSlot {
     // second copy of the PT state (ping-pong of the fused sweep)
     F_A_P, F_A_V1, F_A_V2, F_A_V3, F_A_T11, F_A_T22, F_A_T33, F_A_T12, F_A_T13, F_A_T23,
     F_PRES,  // pressure of the residual evaluation (traction-slaved boundary cells)
+    F_LOAD,  // free-surface load on the top cells
     F_NSLOTS
 };
 
@@ -172,6 +173,7 @@ int slot_of(int field) {
         case SPH_FIELD_TII: return F_TII;
         case SPH_FIELD_RHO: return F_RHO;
         case SPH_FIELD_ETA_PL: return F_ETA_PL;
+        case SPH_FIELD_TOP_LOAD: return F_LOAD;
         default: return -1;
     }
 }
@@ -199,6 +201,9 @@ KP<T> make_kp(Ctx& c, State<T>& s) {
     p.tau_C = T(q.tau_C); p.n_exp = T(c.cur_n); p.relax = T(q.relax); p.edot_bg = T(q.edot_bg);
     p.sig2 = T(q.sig_bc[1]); p.sig3 = T(q.sig_bc[2]);
     p.traction = q.bc == SPH_BC_STRESS ? 1 : 0;
+    p.fs = q.bc == SPH_BC_FREE_SURFACE ? 1 : 0;
+    p.fs_kappa = T(q.fs_kappa);
+    p.top_load = s.f[F_LOAD];
     p.red = c.red;
     return p;
 }
@@ -228,8 +233,8 @@ int ew_blocks(long long n) { return (int)std::min<long long>((n + 255) / 256, 15
 
 // ---------------------------------------------------------------------------
 // boundary-condition programs (the reference's BC kernels in call order)
-BcOp op(int field, int kind, int cd = 0, double c0 = 0.0, double c1 = 0.0) {
-    BcOp o; o.field = field; o.kind = kind; o.cd = cd; o.c0 = c0; o.c1 = c1;
+BcOp op(int field, int kind, int cd = 0, double c0 = 0.0, double c1 = 0.0, int side = -1) {
+    BcOp o; o.field = field; o.kind = kind; o.cd = cd; o.c0 = c0; o.c1 = c1; o.side = side;
     return o;
 }
 BcStage stage(int dim, std::initializer_list<BcOp> ops) {
@@ -252,7 +257,7 @@ int build_bc(Ctx& c) {
     bool ok = s0.dim == 0 && c.xg_fuse;
     for (int i = 0; ok && i < s0.nops; ++i) {
         const BcOp& op = s0.op[i];
-        if (op.field < 0 || op.field > 2 || (mask >> op.field & 1)) { ok = false; break; }
+        if (op.field < 0 || op.field > 2 || (mask >> op.field & 1) || op.side >= 0) { ok = false; break; }
         switch (op.kind) {
             case BC_NEG: case BC_LIN2M: xg[op.field] = -1.f; break;
             case BC_COPY: xg[op.field] = 1.f; break;
@@ -294,6 +299,14 @@ int build_bc_program(Ctx& c) {
         c.bc_run.push_back(c.bc[0]);
         c.bc_run.push_back(stage(1, {op(0, BC_COPY), op(2, BC_COPY), op(1, BC_STRESS_SRC)}));
         c.bc_run.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY), op(2, BC_STRESS_SRC)}));
+        return SPH_OK;
+    }
+    if (q.bc == SPH_BC_FREE_SURFACE) {  // free slip but at the top x1 face; its ghost after the copies
+        if (q.geometry != SPH_GEOM_SPHERICAL) return fail(SPH_ERR_UNSUPPORTED, "SPH_BC_FREE_SURFACE is spherical only");
+        c.bc.push_back(stage(0, {op(0, BC_NEG, 0, 0.0, 0.0, 0), op(1, BC_COPY), op(2, BC_COPY)}));
+        c.bc.push_back(stage(0, {op(0, BC_STRESS, 0, 0.0, 0.0, 1)}));
+        c.bc.push_back(stage(1, {op(0, BC_COPY), op(1, BC_NEG), op(2, BC_COPY)}));
+        c.bc.push_back(stage(2, {op(0, BC_COPY), op(1, BC_COPY), op(2, BC_NEG)}));
         return SPH_OK;
     }
     if (q.bc != SPH_BC_DIAPIR) return fail(SPH_ERR_INVALID, "unknown bc");
@@ -461,7 +474,7 @@ int init_fields(Ctx& c) {
 int sync32(Ctx& c) {
     if (!c.has32 || !c.stale32) return SPH_OK;
     const long long vol = c.d.vol;
-    const int slots[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23, F_ETA, F_ETA_INI, F_ETA_SM, F_DT_R, F_TII, F_RHO, F_ETA_PL};
+    const int slots[] = {F_P, F_V1, F_V2, F_V3, F_T11, F_T22, F_T33, F_T12, F_T13, F_T23, F_ETA, F_ETA_INI, F_ETA_SM, F_DT_R, F_TII, F_RHO, F_ETA_PL, F_LOAD};
     for (int sl : slots) k_convert<float, double><<<ew_blocks(vol), 256, 0, c.stream>>>(c.s32.f[sl], c.s64.f[sl], vol);
     CK(cudaGetLastError());
     c.stale32 = false;
@@ -702,7 +715,7 @@ int residual64_g(Ctx& c, double out[7], bool eta_from_law) {
     r.eta = const_cast<double*>(eta_eff);
     r.t11 = s.f[F_Q11]; r.t22 = s.f[F_Q22]; r.t33 = s.f[F_Q33]; r.t12 = s.f[F_Q12]; r.t13 = s.f[F_Q13]; r.t23 = s.f[F_Q23];
     k_tau_visc<double, G><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(r);
-    if (r.traction) {
+    if (r.traction || r.fs) {
         k_traction_pressure<double><<<grid_cells(c.d), blk2d(), 0, c.stream>>>(r, s.f[F_PRES]);
         r.P = s.f[F_PRES];
     }
@@ -745,6 +758,12 @@ int compute_f_scale(Ctx& c) {
     const sph_params& q = c.prm;
     double f = slot_val(c, 0) * std::fabs(q.g);
     if (q.bc == SPH_BC_STRESS) f = std::max(f, std::max(std::fabs(q.sig_bc[1]), std::fabs(q.sig_bc[2])) / q.l1);
+    if (q.bc == SPH_BC_FREE_SURFACE) {  // the surface load's force scale, max|q| / l1
+        CK(cudaMemsetAsync(c.red, 0, sizeof(unsigned long long) * kRedSlots, c.stream));
+        launch_maxabs<double>(c, c.s64.f[F_LOAD], nullptr, 0);
+        if ((rc = fetch_red(c))) return rc;
+        f = std::max(f, slot_val(c, 0) / q.l1);
+    }
     c.f_scale = f > 0.0 ? f : 1.0;
     return SPH_OK;
 }
@@ -972,6 +991,7 @@ int usable(const Ctx& c) {
 KP<float> make_kp_corr(Ctx& c) {
     KP<float> q = make_kp<float>(c, c.s32);
     q.sig2 = 0.f;
+    q.top_load = nullptr;
     q.sig3 = 0.f;
     return q;
 }
@@ -1572,7 +1592,8 @@ int check_params(const sph_params* p) {
     if (p->geometry < 0 || p->geometry > 2) return fail(SPH_ERR_INVALID, "geometry");
     if (p->precision < 0 || p->precision > 2) return fail(SPH_ERR_INVALID, "precision");
     if (p->rheology < 0 || p->rheology > 3) return fail(SPH_ERR_INVALID, "rheology");
-    if (p->bc < 0 || p->bc > 2) return fail(SPH_ERR_INVALID, "bc");
+    if (p->bc < 0 || p->bc > 3) return fail(SPH_ERR_INVALID, "bc");
+    if (p->bc == SPH_BC_FREE_SURFACE && p->geometry != SPH_GEOM_SPHERICAL) return fail(SPH_ERR_UNSUPPORTED, "SPH_BC_FREE_SURFACE is spherical only");
     if (p->n1 < 5 || p->n2 < 5 || p->n3 < 5) return fail(SPH_ERR_INVALID, "grid needs at least 5 cells per axis");
     // x2 and x3 index the launch grids' y and z dimensions (at most 65535 blocks each)
     if (p->n2 >= 65535 || p->n3 >= 65535) return fail(SPH_ERR_INVALID, "n2 and n3 must be below 65535");
@@ -1712,6 +1733,7 @@ int sph_create(const sph_params* prm, void** out) {
     if (const char* e = std::getenv("SPH_NO_GRAPHS")) c->use_graphs = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_TMA")) c->use_tma = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_SWEEP_X2")) c->use_x2 = std::atoi(e) != 0;
+    if (q.bc == SPH_BC_FREE_SURFACE) c->use_x2 = false;  // the paired-FP32 sweep has no free-surface top cell
     if (const char* e = std::getenv("SPH_NO_PDL")) c->use_pdl = std::atoi(e) == 0;
     if (const char* e = std::getenv("SPH_NO_XGHOST")) c->xg_fuse = std::atoi(e) == 0;
     if ((rc = build_bc(*c))) return cleanup(rc);
@@ -1921,6 +1943,8 @@ enum AdjSlot {
 };
 
 static int adj_alloc(Ctx* c) {
+    if (c->prm.bc == SPH_BC_FREE_SURFACE)  // no transposed free-surface BC or top-cell pressure
+        return fail(SPH_ERR_UNSUPPORTED, "the adjoint is not built for SPH_BC_FREE_SURFACE");
     if (c->adj) return SPH_OK;
     const size_t b = sizeof(double) * (size_t)c->d.vol * AJ_COUNT;
     if (cudaMalloc((void**)&c->adj, b) != cudaSuccess) return fail(SPH_ERR_NOMEM, "adjoint arrays");
@@ -2079,7 +2103,7 @@ int sph_set_field(void* h, int32_t field, const double* host, int64_t count) {
     if (rc) return rc;
     rc = copy_field(c, field, nullptr, host, count);
     if (rc) return rc;
-    if (field == SPH_FIELD_RHO) return compute_f_scale(*c);
+    if (field == SPH_FIELD_RHO || field == SPH_FIELD_TOP_LOAD) return compute_f_scale(*c);
     return SPH_OK;
 }
 

@@ -43,10 +43,13 @@ def oracle_state(p):
     return oracle.Sph.from_params(p) if p.geometry == 0 else oracle.CC.from_params(p)
 
 
-def run_case(p, k, random_start, seed=0):
-    """k GPU correction sweeps and the oracle's from the same start; returns the group errors."""
+def run_case(p, k, random_start, seed=0, setup=None):
+    """k GPU correction sweeps and the oracle's from the same start; returns the group errors.
+    setup(solver): called before the correction problem is prepared (e.g. to set a field)."""
     rng = np.random.default_rng(seed)
     with S.Solver(p) as sv:
+        if setup:
+            setup(sv)
         if random_start:
             for f in STATE:
                 a = sv.corr_get(f)

@@ -233,6 +233,12 @@ class EllipsePlateau:
     eta_ratio: float = 1e-2         # crust / mantle viscosity
     eta_air: float = 1e-3           # air / mantle viscosity
     dmp: float = 4.5
+    # "sticky_air": an air layer of air_km above the reference surface carries the topography;
+    # "free_surface": the domain ends at the reference surface, whose traction carries the load of
+    # the plateau's isostatic topography h = (ρ_mantle - ρ_crust)/ρ_crust (h_crust - h_crust,outside)
+    # (SPH_BC_FREE_SURFACE) with the stabilisation term θ Δt ρ_crust g V_r
+    top: str = "sticky_air"
+    fs_theta_dt: float = 0.5        # θ Δt of the stabilisation, in units of η_mantle / (ρ_mantle g depth)
 
     def params(self, precision: str = "mixed", **kw) -> Params:
         """Spherical shell r in [R - depth, R + air], scaled by the depth; stress-free
@@ -240,14 +246,16 @@ class EllipsePlateau:
         from . import default_params
 
         L = self.depth_km
-        r0, r1 = (self.R_km - self.depth_km) / L, (self.R_km + self.air_km) / L
+        fs = self.top == "free_surface"
+        r0, r1 = (self.R_km - self.depth_km) / L, (self.R_km + (0.0 if fs else self.air_km)) / L
         ext = math.radians(self.extent_deg)
         p = default_params("spherical")
-        vr = 1.0 / min(self.eta_ratio, self.eta_air)
-        set_params(p, precision=precision, bc="free_slip", rheology="edot_power_relax", n_exp=self.n_exp, relax=0.5,
-                   edot_bg=1.0, init="none", n1=self.nr, n2=self.nth, n3=self.nph, c1=0.5 * (r0 + r1), l1=r1 - r0,
-                   c2=math.pi / 2, l2=ext, c3=0.0, l3=ext, l_ref=r1 - r0, r=self.R_km / L, dmp=self.dmp, g=1.0,
-                   vr=vr, vpdt=0.0, eta0=1.0, rho0=1.0, sh=0.0, incl_linear=1)
+        vr = 1.0 / (self.eta_ratio if fs else min(self.eta_ratio, self.eta_air))
+        set_params(p, precision=precision, bc="free_surface" if fs else "free_slip", rheology="edot_power_relax",
+                   n_exp=self.n_exp, relax=0.5, edot_bg=1.0, init="none", n1=self.nr, n2=self.nth, n3=self.nph,
+                   c1=0.5 * (r0 + r1), l1=r1 - r0, c2=math.pi / 2, l2=ext, c3=0.0, l3=ext, l_ref=r1 - r0, r=self.R_km / L,
+                   dmp=self.dmp, g=1.0, vr=vr, vpdt=0.0, eta0=1.0, rho0=1.0, sh=0.0, incl_linear=1,
+                   fs_kappa=self.fs_theta_dt * self.rho_crust / self.rho_mantle if fs else 0.0)
         set_params(p, **kw)
         return p
 
@@ -295,8 +303,26 @@ class EllipsePlateau:
         eta[crust] = self.eta_ratio
         eta[air] = self.eta_air
         phase = np.where(crust, 0.0, 1.0)
-        return {"RHO": np.asfortranarray(rho), "ETA_INI": np.asfortranarray(eta), "ETA": np.asfortranarray(eta),
-                "PHASE": np.asfortranarray(phase)}
+        out = {"RHO": np.asfortranarray(rho), "ETA_INI": np.asfortranarray(eta), "ETA": np.asfortranarray(eta),
+               "PHASE": np.asfortranarray(phase)}
+        if self.top == "free_surface":
+            out["TOP_LOAD"] = np.asfortranarray(self.surface_load(p))
+        return out
+
+    def topography_km(self, th: np.ndarray, ph: np.ndarray) -> np.ndarray:
+        """Isostatic (Airy) elevation of the plateau: h = (ρ_mantle - ρ_crust)/ρ_crust times the crust
+        thickness in excess of the outside value."""
+        excess = self.crust_thickness_km(th, ph) - self.crust_km[0]
+        return (self.rho_mantle - self.rho_crust) / self.rho_crust * excess
+
+    def surface_load(self, p: Params) -> np.ndarray:
+        """SPH_FIELD_TOP_LOAD of the free-surface top: ρ_crust g h on the top cells (units ρ_mantle g depth),
+        zero below."""
+        x2, x3 = linspace(p.c2, p.l2, p.n2), linspace(p.c3, p.l3, p.n3)
+        T, F = np.meshgrid(x2, x3, indexing="ij")
+        q = np.zeros((p.n1, p.n2, p.n3), order="F")
+        q[p.n1 - 1] = self.rho_crust / self.rho_mantle * self.topography_km(T, F) / self.depth_km
+        return q
 
 
 def ellipse_solver(setup: EllipsePlateau, precision: str = "mixed", **kw) -> Solver:

@@ -58,3 +58,30 @@ def test_mixed_solve_on_a_reduced_plateau_grid():
         res = sv.solve(tol=1e-8, maxiter=400000, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=30, inner_max=20000)
         # a viscosity contrast of 1e3 (air / mantle) and n = 3: a bounded budget, an order of magnitude
         assert np.isfinite(res.residual) and res.residual < 0.1 * r0, (r0, res.residual, res.status)
+
+
+def test_free_surface_fields_and_load():
+    """top="free_surface": no air cells, the domain ends at the reference surface, and the top cells
+    carry the isostatic load of the plateau (70 km crust inside: (3300-2800)/2800 x 35 km = 6.25 km of
+    topography, ρ_crust g h in units of ρ_mantle g depth); outside the taper the load is zero"""
+    e = PL.EllipsePlateau(nr=41, nth=21, nph=21, top="free_surface")
+    p = e.params()
+    assert p.bc == S.BC["free_surface"] and p.fs_kappa > 0.0
+    assert abs((p.c1 + 0.5 * p.l1) - e.R_km / e.depth_km) < 1e-12
+    f = e.fields(p)
+    assert f["RHO"].min() > 0.5  # crust and mantle only
+    q = f["TOP_LOAD"]
+    assert np.all(q[:-1] == 0.0)
+    peak = e.rho_crust / e.rho_mantle * (e.rho_mantle - e.rho_crust) / e.rho_crust * 35.0 / e.depth_km
+    assert abs(q[-1, 10, 10] - peak) < 1e-12 and q[-1, 0, 0] == 0.0
+
+
+@pytest.mark.gpu
+def test_mixed_solve_on_a_reduced_free_surface_plateau():
+    e = PL.EllipsePlateau(nr=47, nth=31, nph=31, top="free_surface")
+    with PL.ellipse_solver(e, "mixed") as sv:
+        r0 = sv.residual()["err"]
+        res = sv.solve(tol=1e-8, maxiter=400000, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=30, inner_max=20000)
+        assert np.isfinite(res.residual) and res.residual < 0.1 * r0, (r0, res.residual, res.status)
+        v = [sv.get(f) for f in ("V1", "V2", "V3")]
+    assert all(np.isfinite(a).all() for a in v) and max(np.abs(a).max() for a in v) > 0.0

@@ -449,16 +449,27 @@ def run_ours(args) -> None:
     if args.plateau_sweeps > 0:
         from sphericalstokes_gb300 import plateau as PL
 
-        ep = PL.EllipsePlateau()
+        ep = PL.EllipsePlateau(top=args.plateau_top)
         with PL.ellipse_solver(ep, "mixed") as sv:
             sv.sweep(args.warmup)
             ms = sv.sweep(args.plateau_sweeps)
+            r_solve = None
+            if args.plateau_solve_sweeps > 0:  # a budget-bounded mixed solve from the initial state
+                sv.sweep_apply()
+                r0 = sv.residual()["err"]
+                r_solve = sv.solve(tol=1e-8, maxiter=args.plateau_solve_sweeps, nout=100, criterion="residual", inner_rtol=0.1,
+                                   max_outer=1000, inner_max=60000)
         cells = ep.nr * ep.nth * ep.nph
-        plateau_info = {"grid": [ep.nr, ep.nth, ep.nph], "sweeps": args.plateau_sweeps,
+        plateau_info = {"grid": [ep.nr, ep.nth, ep.nph], "sweeps": args.plateau_sweeps, "top": ep.top,
                         "ms_per_sweep": round(ms / args.plateau_sweeps, 4),
                         "teff_gbs": round(26 * cells * 4 / (ms / args.plateau_sweeps * 1e-3) / 1e9, 1),
-                        "setup": "elliptical plateau on a 40°x40° shell, 200 km deep + 20 km sticky air, n=3 crust over "
-                                 "linear mantle (ratio 1e-2), seeded ±2% density field; FP32 correction sweeps"}
+                        "setup": ("elliptical plateau on a 40°x40° shell, 200 km deep, n=3 crust over linear mantle (ratio 1e-2), "
+                                  "seeded ±2% density field; " +
+                                  ("free-surface-stabilised top carrying the isostatic topography load" if ep.top == "free_surface"
+                                   else "20 km sticky air") + "; FP32 correction sweeps")}
+        if r_solve is not None:
+            plateau_info["solve"] = {"sweeps": r_solve.iters, "outer": r_solve.outer, "seconds": round(r_solve.seconds, 2),
+                                     "initial_residual": r0, "residual": r_solve.residual, "status": r_solve.status}
 
     batch_info = None
     if args.batch > 0:
@@ -568,6 +579,9 @@ def main():
     ap.add_argument("--batch-threads", type=int, default=16)
     ap.add_argument("--plateau-sweeps", type=int, default=200,
                     help="sweeps timed on the 511x255x255 elliptical-plateau grid (0: skip)")
+    ap.add_argument("--plateau-top", default="free_surface", choices=["free_surface", "sticky_air"])
+    ap.add_argument("--plateau-solve-sweeps", type=int, default=0,
+                    help="sweep budget of a mixed solve of the plateau from its initial state (0: skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

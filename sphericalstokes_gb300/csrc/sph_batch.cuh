@@ -35,6 +35,7 @@ struct BatchSweep {
 template <int G>
 __global__ void __launch_bounds__(FNT, 3) k_fused_tma_batch(const BatchSweep* __restrict__ b, const int4* __restrict__ items,
                                                              const int* __restrict__ active, int a) {
+    pdl_wait();  // as k_fused_tma: no early release of the next grid
     const int4 it = items[blockIdx.x];
     if (!active[it.x]) return;  // whole block: no barrier is reached
     const BatchSweep& s = b[it.x];
@@ -46,6 +47,7 @@ __global__ void __launch_bounds__(FNT, 3) k_fused_tma_batch(const BatchSweep* __
 template <int G>
 __global__ void k_bc_batch(const BatchSweep* __restrict__ b, const int4* __restrict__ items, const int* __restrict__ active, int a,
                            int t) {
+    pdl_enter();  // as k_bc
     const int4 it = items[blockIdx.x];
     if (!active[it.x]) return;
     const BatchSweep& s = b[it.x];

@@ -1436,6 +1436,8 @@ int batch_lockstep(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph
         CK(cudaStreamSynchronize(b.c->stream));
     }
     const int nout = batch_nout(opts[0]);
+    bool pdl = true;  // programmatic dependent launches inside the round's graph (off if any solve has them off)
+    for (int32_t i = 0; i < n; ++i) pdl = pdl && static_cast<Ctx*>(ctxs[i])->use_pdl;
     BatchDev dev;
     struct Restore {  // every context back on its own stream, on every return path
         std::vector<BatchSolve>& bs;
@@ -1500,13 +1502,17 @@ int batch_lockstep(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph
         CK(cudaStreamBeginCapture(dev.stream, cudaStreamCaptureModeThreadLocal));
         for (int sw = 0; sw < nout; ++sw) {
             const int a = sw & 1;
-            if (fz_n[SPH]) k_fused_tma_batch<SPH><<<(unsigned)fz_n[SPH], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[SPH], dev.active, a);
-            if (fz_n[CYL]) k_fused_tma_batch<CYL><<<(unsigned)fz_n[CYL], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[CYL], dev.active, a);
-            if (fz_n[CART]) k_fused_tma_batch<CART><<<(unsigned)fz_n[CART], FNT, fused_tma_smem_bytes(), dev.stream>>>(dev.entries, dev.items + fz_off[CART], dev.active, a);
+            // programmatic dependent launches, as the single-grid sweep: each launch overlaps the
+            // tail of the one before (the kernels wait on it before touching memory)
+            const BatchSweep* E = dev.entries;
+            const int* act_d = dev.active;
+            if (fz_n[SPH]) launch_pdl(pdl, k_fused_tma_batch<SPH>, dim3((unsigned)fz_n[SPH]), dim3(FNT), fused_tma_smem_bytes(), dev.stream, E, dev.items + fz_off[SPH], act_d, a);
+            if (fz_n[CYL]) launch_pdl(pdl, k_fused_tma_batch<CYL>, dim3((unsigned)fz_n[CYL]), dim3(FNT), fused_tma_smem_bytes(), dev.stream, E, dev.items + fz_off[CYL], act_d, a);
+            if (fz_n[CART]) launch_pdl(pdl, k_fused_tma_batch<CART>, dim3((unsigned)fz_n[CART]), dim3(FNT), fused_tma_smem_bytes(), dev.stream, E, dev.items + fz_off[CART], act_d, a);
             for (int t = 0; t < kBatchMaxBc; ++t) {
-                if (bc_n[SPH][t]) k_bc_batch<SPH><<<(unsigned)bc_n[SPH][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[SPH][t], dev.active, a, t);
-                if (bc_n[CYL][t]) k_bc_batch<CYL><<<(unsigned)bc_n[CYL][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[CYL][t], dev.active, a, t);
-                if (bc_n[CART][t]) k_bc_batch<CART><<<(unsigned)bc_n[CART][t], blk2d(), 0, dev.stream>>>(dev.entries, dev.items + bc_off[CART][t], dev.active, a, t);
+                if (bc_n[SPH][t]) launch_pdl(pdl, k_bc_batch<SPH>, dim3((unsigned)bc_n[SPH][t]), blk2d(), 0, dev.stream, E, dev.items + bc_off[SPH][t], act_d, a, t);
+                if (bc_n[CYL][t]) launch_pdl(pdl, k_bc_batch<CYL>, dim3((unsigned)bc_n[CYL][t]), blk2d(), 0, dev.stream, E, dev.items + bc_off[CYL][t], act_d, a, t);
+                if (bc_n[CART][t]) launch_pdl(pdl, k_bc_batch<CART>, dim3((unsigned)bc_n[CART][t]), blk2d(), 0, dev.stream, E, dev.items + bc_off[CART][t], act_d, a, t);
             }
         }
         cudaError_t e = cudaStreamEndCapture(dev.stream, &g);

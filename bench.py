@@ -191,6 +191,31 @@ def cpu_baseline(n: int, seconds: float = 15.0, threads: int | None = None) -> d
             "sample": f"{it} FP64 PT iterations of the {n}^3 workload ({dt * 1e3:.1f} ms each)"}
 
 
+def cpu_time_to_tol(n: int, tol: float = 1e-8, check: int = 1000, max_iters: int = 5_000_000) -> dict:
+    """configs[0] on the CPU: plain FP64 PT of the oracle port (all host threads) on the n^3 spherical
+    sector, linear viscosity (inclusion 1e-3, Δρ = -1), free slip on all faces, the reference's PT
+    step, iterated to FP64 residual `tol` (checked every `check` iterations)."""
+    import oracle
+
+    p = reference_params(n)
+    p.bc, p.rheology, p.n_exp, p.sig_bc = 1, 0, 1.0, (0.0, 0.0, 0.0)
+    o = oracle.Sph.from_params(p)
+    t0 = time.perf_counter()
+    it, err, hist = 0, float("inf"), []
+    while it < max_iters:
+        o.iterate(check)
+        it += check
+        err = o.residual()["err"]
+        hist.append([it, round(time.perf_counter() - t0, 2), err])
+        if not (err == err) or err < tol:
+            break
+    return {"n": n, "tol": tol, "iterations": it, "seconds": round(time.perf_counter() - t0, 2), "residual": err,
+            "converged": bool(err < tol), "cores": oracle.num_threads(), "history_every": max(1, len(hist) // 20),
+            "curve_iter_s_residual": hist[:: max(1, len(hist) // 20)] + hist[-1:],
+            "setup": "linear free-slip sector, inclusion η 1e-3 Δρ -1 r 0.1, reference PT step, residual every "
+                     f"{check} iterations (the reference's Threads backend is absent: oracle port of its kernels)"}
+
+
 def run_reference(args) -> None:
     """The reference's CPU implementation of the path (the oracle port of its kernels, all host
     threads) on the same workload.  A step is one FP64 PT iteration over a sample of the grid:
@@ -231,6 +256,8 @@ def run_reference(args) -> None:
         "cpu_baseline": {"value": round(teff, 3), "unit": "GB/s", "cores": oracle.num_threads(), "kind": "port", "sample": sample},
         "e2e": {"value": round(teff, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if args.cpu_solve_n > 0:
+        line["cpu_time_to_tol"] = cpu_time_to_tol(args.cpu_solve_n)
     print(json.dumps(line), flush=True)
 
 
@@ -558,6 +585,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0, help="target length of the --impl reference run")
+    ap.add_argument("--cpu-solve-n", type=int, default=0,
+                    help="--impl reference: also iterate the linear n^3 sector (configs[0]) to residual 1e-8 on the CPU")
     ap.add_argument("--prep-sweeps", type=int, default=500)
     ap.add_argument("--max-sweeps", type=int, default=2_000_000)
     ap.add_argument("--inner-rtol", type=float, default=1e-2)

@@ -66,7 +66,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 template <int G, int MODE>
 __global__ void __launch_bounds__(FNT, 3) k_fused(KP<float> p, FusedOut<float> o, int kchunk) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     FusedSmem& S = *reinterpret_cast<FusedSmem*>(smem_raw);
     enum { IP = 0, I11, I22, I33, I12, I13, I23, IX };  // old-ring / stress-ring field slots (IX: rP | ρ, or DT_R)
 

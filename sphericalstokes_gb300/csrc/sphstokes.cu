@@ -1450,50 +1450,71 @@ int batch_lockstep(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph
     CK(cudaEventRecord(dev.e0, dev.stream));
     for (BatchSolve& b : bs) { int rc = sync64(*b.c); if (rc) return rc; }
 
-    // work lists: blocks of every solve's fused sweep, BC stages and inner test, per geometry
+    // work lists: blocks of the member solves' fused sweeps, BC stages and inner tests, per geometry
     std::vector<BatchSweep> host((size_t)n);
     std::vector<int4> items;
     size_t fz_off[3], fz_n[3], nm_off[3], nm_n[3], bc_off[3][kBatchMaxBc], bc_n[3][kBatchMaxBc];
-    for (int g = 0; g < 3; ++g) {
-        fz_off[g] = items.size();
-        for (int32_t i = 0; i < n; ++i) {
-            Ctx& c = *bs[i].c;
-            if (c.prm.geometry != g) continue;
-            const int kc = fused_chunk(c);
-            const int gx = (c.d.n1 + FTX - 1) / FTX, gy = (c.d.n2 + FTY - 1) / FTY, gz = (c.d.n3 + kc - 1) / kc;
-            for (int z = 0; z < gz; ++z) for (int y = 0; y < gy; ++y) for (int x = 0; x < gx; ++x) items.push_back(make_int4(i, x, y, z));
-        }
-        fz_n[g] = items.size() - fz_off[g];
-        for (int t = 0; t < kBatchMaxBc; ++t) {
-            bc_off[g][t] = items.size();
-            for (int32_t i = 0; i < n; ++i) {
+    size_t items_cap = 0, members = 0;
+    auto build_lists = [&]() -> int {
+        items.clear();
+        members = 0;
+        std::vector<int> mem;
+        for (int32_t i = 0; i < n; ++i)
+            if (bs[i].st != BatchSolve::DONE) mem.push_back(i);
+        members = mem.size();
+        for (int g = 0; g < 3; ++g) {
+            fz_off[g] = items.size();
+            for (int i : mem) {
                 Ctx& c = *bs[i].c;
-                const int first = c.xg_mask ? 1 : 0;
-                if (c.prm.geometry != g || first + t >= (int)c.bc_run.size()) continue;
-                const BcStage& st = c.bc_run[first + t];
-                const int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1, ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
-                for (int v = 0; v < (ev + 7) / 8; ++v) for (int u = 0; u < (eu + 31) / 32; ++u) items.push_back(make_int4(i, u, v, 0));
+                if (c.prm.geometry != g) continue;
+                const int kc = fused_chunk(c);
+                const int gx = (c.d.n1 + FTX - 1) / FTX, gy = (c.d.n2 + FTY - 1) / FTY, gz = (c.d.n3 + kc - 1) / kc;
+                for (int z = 0; z < gz; ++z) for (int y = 0; y < gy; ++y) for (int x = 0; x < gx; ++x) items.push_back(make_int4(i, x, y, z));
             }
-            bc_n[g][t] = items.size() - bc_off[g][t];
+            fz_n[g] = items.size() - fz_off[g];
+            for (int t = 0; t < kBatchMaxBc; ++t) {
+                bc_off[g][t] = items.size();
+                for (int i : mem) {
+                    Ctx& c = *bs[i].c;
+                    const int first = c.xg_mask ? 1 : 0;
+                    if (c.prm.geometry != g || first + t >= (int)c.bc_run.size()) continue;
+                    const BcStage& st = c.bc_run[first + t];
+                    const int eu = st.dim == 0 ? c.d.n2 + 1 : c.d.n1 + 1, ev = st.dim == 2 ? c.d.n2 + 1 : c.d.n3 + 1;
+                    for (int v = 0; v < (ev + 7) / 8; ++v) for (int u = 0; u < (eu + 31) / 32; ++u) items.push_back(make_int4(i, u, v, 0));
+                }
+                bc_n[g][t] = items.size() - bc_off[g][t];
+            }
+            nm_off[g] = items.size();
+            for (int i : mem) {
+                Ctx& c = *bs[i].c;
+                if (c.prm.geometry != g) continue;
+                const dim3 gv = grid_vel(c.d);
+                for (unsigned z = 0; z < gv.z; ++z) for (unsigned y = 0; y < gv.y; ++y) for (unsigned x = 0; x < gv.x; ++x)
+                    items.push_back(make_int4(i, (int)x, (int)y, (int)z));
+            }
+            nm_n[g] = items.size() - nm_off[g];
         }
-        nm_off[g] = items.size();
-        for (int32_t i = 0; i < n; ++i) {
-            Ctx& c = *bs[i].c;
-            if (c.prm.geometry != g) continue;
-            const dim3 gv = grid_vel(c.d);
-            for (unsigned z = 0; z < gv.z; ++z) for (unsigned y = 0; y < gv.y; ++y) for (unsigned x = 0; x < gv.x; ++x)
-                items.push_back(make_int4(i, (int)x, (int)y, (int)z));
+        if (items.size() > items_cap) {
+            CK(cudaStreamSynchronize(dev.stream));
+            if (dev.items) cudaFree(dev.items);
+            dev.items = nullptr;
+            if (cudaMalloc((void**)&dev.items, sizeof(int4) * std::max<size_t>(items.size(), 1)) != cudaSuccess) {
+                cudaGetLastError();
+                return fail(SPH_ERR_NOMEM, "batched solve: device work lists");
+            }
+            items_cap = items.size();
         }
-        nm_n[g] = items.size() - nm_off[g];
-    }
+        CK(cudaMemcpyAsync(dev.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, dev.stream));
+        CK(cudaStreamSynchronize(dev.stream));  // the host list is rebuilt in place next time
+        return SPH_OK;
+    };
     if (cudaMalloc((void**)&dev.entries, sizeof(BatchSweep) * n) != cudaSuccess || cudaMalloc((void**)&dev.active, sizeof(int) * n) != cudaSuccess ||
-        cudaMalloc((void**)&dev.red, sizeof(unsigned long long) * n) != cudaSuccess ||
-        cudaMalloc((void**)&dev.items, sizeof(int4) * std::max<size_t>(items.size(), 1)) != cudaSuccess) {
+        cudaMalloc((void**)&dev.red, sizeof(unsigned long long) * n) != cudaSuccess) {
         cudaGetLastError();
         return fail(SPH_ERR_NOMEM, "batched solve: device work lists");
     }
-    CK(cudaMemcpyAsync(dev.items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, dev.stream));
     CK(cudaMemsetAsync(dev.entries, 0, sizeof(BatchSweep) * n, dev.stream));
+    if (int rc = build_lists()) return rc;
     std::vector<int> act((size_t)n, 0);
 
     // one round: nout sweeps of every active solve (arrangement a = s & 1 read by sweep s)
@@ -1552,10 +1573,17 @@ int batch_lockstep(void* const* ctxs, int32_t n, const sph_solve_opts* opts, sph
                 any = true;
             }
         }
-        for (const BatchSolve& b : bs) pending |= b.st != BatchSolve::DONE;
+        size_t open_solves = 0;
+        for (const BatchSolve& b : bs) open_solves += b.st != BatchSolve::DONE;
+        pending = open_solves > 0;
         if (!any) {
             if (!pending) break;
             continue;
+        }
+        // finished solves leave the work list once they are half of it (a new list, a new graph)
+        if (2 * open_solves <= members && open_solves < members) {
+            if (dev.graph) { CK(cudaStreamSynchronize(dev.stream)); cudaGraphExecDestroy(dev.graph); dev.graph = nullptr; }
+            if ((rc = build_lists())) return rc;
         }
         if (!dev.graph && (rc = capture())) return rc;
         CK(cudaMemcpyAsync(dev.active, act.data(), sizeof(int) * n, cudaMemcpyHostToDevice, dev.stream));

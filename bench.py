@@ -58,17 +58,29 @@ sys.path.insert(0, str(ROOT))
 METRIC = "T_eff GB/s and time-to-1e-8 at 255³ n=3: FP32+FP64-refine vs FP64 PT, 1 GB300"
 
 
-def workload_params(n: int, precision: str, tuned: bool = False):
+def workload_params(n: int, precision: str, tuned: bool = False, dmp: float | None = None):
     """The n=3 spherical-sector workload.  ``tuned``: the PT parameters of the
     time-to-tolerance runs, the same for plain FP64 and for the mixed solve —
-    two passes of the ηSM max filter, twice the reference pseudo-step, damping 3."""
+    two passes of the ηSM max filter, twice the reference pseudo-step, damping 3.
+    ``dmp``: the damping (bulk/shear pseudo-modulus ratio ×2) instead of the set's."""
     import sphericalstokes_gb300 as S
 
     p = S.sector_params(n, bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,
                         sig_bc=(0.0, 0.5, -0.5), incl_linear=1, precision=precision)
     if tuned:
         S.set_params(p, etasm_passes=2, vpdt=2.0 * p.vpdt, dmp=3.0)
+    if dmp is not None:
+        S.set_params(p, dmp=dmp)
     return p
+
+
+def pt_parameters(p, n: int) -> str:
+    """The PT parameters of a solve, stated against the reference's step."""
+    import sphericalstokes_gb300 as S
+
+    ref = S.sector_params(n).vpdt
+    return (f"pseudo-step {p.vpdt / ref:g}x the reference's (CFL = 1/(2+4.5 log10 vr) of the smallest spacing), "
+            f"dmp {p.dmp:g}, ηSM max filter {p.etasm_passes} pass(es)")
 
 
 def workload_desc(n: int) -> str:
@@ -290,7 +302,8 @@ def time_to_tolerance(args) -> dict:
     n = args.solve_n
     info: dict = {"n": n, "tol": 1e-8}
     vel = {}
-    p = workload_params(n, "mixed", tuned=args.tuned)
+    p = workload_params(n, "mixed", tuned=args.tuned, dmp=args.dmp)
+    info["pt_parameters"] = pt_parameters(p, n) + " (both solves)"
     with S.Solver(p) as sv:
         r = sv.solve(tol=1e-8, maxiter=args.max_sweeps, nout=100, criterion="residual", inner_rtol=args.inner_rtol,
                      max_outer=args.max_outer, inner_max=args.inner_max, warm_tol=args.warm_tol, hist_cap=1_000_000)
@@ -300,7 +313,7 @@ def time_to_tolerance(args) -> dict:
     info["mixed"] = {"seconds": round(r.seconds, 3), "iterations": r.iters, "outer": r.outer, "residual": r.residual,
                      "converged": r.converged, "sweep_s": round(r.sweep_ms * 1e-3, 3), "outer_s": round(r.outer_ms * 1e-3, 3),
                      "curve_s_residual": _curve(ms_m, err_m)}
-    p = workload_params(n, "fp64", tuned=args.tuned)
+    p = workload_params(n, "fp64", tuned=args.tuned, dmp=args.dmp)
     nout = args.fp64_nout
     maxiter = args.fp64_maxiter
     if args.fp64_budget_s > 0:
@@ -328,8 +341,6 @@ def time_to_tolerance(args) -> dict:
     info["rel_velocity_error_mixed_vs_fp64"] = max(float(np.abs(a - b).max()) for a, b in zip(vel["mixed"], vel["fp64"])) / vmax
     info["rel_velocity_error_against"] = ("the converged FP64 solution" if info["fp64"]["converged"]
                                           else f"the last FP64 iterate (residual {info['fp64']['residual']:.2e})")
-    info["pt_parameters"] = ("ηSM max filter 2 passes, pseudo-step 2x the reference CFL, dmp 3 (both solves)" if args.tuned
-                             else "the reference's PT step (CFL = 1/(2+4.5 log10 vr) of the smallest spacing), dmp 4.5 (both solves)")
     return info
 
 
@@ -582,6 +593,8 @@ def main():
                     help="plain FP64 PT iterations timed on the same workload (the FP32 sweep's per-iteration baseline; 0: skip)")
     ap.add_argument("--tuned", type=int, default=1,
                     help="time-to-tolerance PT parameters: 1 the tuned set (2 ηSM passes, 2x step, dmp 3), 0 the reference's")
+    ap.add_argument("--dmp", type=float, default=None,
+                    help="time-to-tolerance damping instead of the parameter set's (both solves)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0, help="target length of the --impl reference run")

@@ -6,13 +6,25 @@ stress ratio uniform in [0, 1]) and its runner over ``sph_batch_solve``.
 
 Each case is one of the reference's diapir setups (SphericalStokes_diapir.jl,
 CylindricalStokes_diapir.jl, CartesianStokes_diapir.jl) with the strain-rate
-power law (linear for n = 1).  The stress ratio s sets the far-field normal
+power law (linear for n = 1).
+
+PT step of the batch (``step_cap``).  The reference's step, CFL = 1/(2 + 4.5 log10 vr)
+of the grid spacing (CylindricalStokes_diapir.jl:250,322), was chosen for vr = 10^2.  A
+velocity node between two cells whose ηSM differ by vr takes the mean of their steps
+(compute_V!, SphericalStokes_diapir.jl:315-327), about vr/2 times the step that the
+stiffer cell's pressure tolerates, so the local Courant number is CFL·sqrt(vr/2): 0.64
+at vr = 10^2, 1.4 at 10^3 and 3.5 at 10^4.  Draws above 10^2 then diverge within a few
+hundred iterations (plain FP64 PT as well as the mixed solve).  ``step_cap`` limits the
+step to 0.64/sqrt(vr/2) of the spacing, the Courant number the reference's own choice
+has at vr = 10^2.  The PT step does not change the discrete equations, only how fast
+(and whether) the iteration reaches their solution.  The stress ratio s sets the far-field normal
 stresses (0, +s/2, -s/2) on the spherical sector and the cylindrical faces; the
 Cartesian scheme has no deviatoric normal stresses to load, so there s is the
 simple-shear rate of the script's own boundary condition.
 """
 from __future__ import annotations
 
+import math
 import time
 
 import numpy as np
@@ -23,8 +35,14 @@ EDGES = (31, 47, 63, 79, 95)
 GEOMETRIES = ("spherical", "cylindrical", "cartesian")
 
 
-def sweep_cases(count: int = 256, seed: int = 0, edges=EDGES, precision: str = "mixed") -> list:
-    """Parameters of ``count`` solves drawn with numpy's PCG64 generator from ``seed``."""
+def capped_cfl(vr: float) -> float:
+    """The reference's CFL = 1/(2 + 4.5 log10 vr), limited to 0.64/sqrt(vr/2) (module docstring)."""
+    return min(1.0 / (2.0 + 4.5 * math.log10(vr)), 0.64 / math.sqrt(0.5 * vr))
+
+
+def sweep_cases(count: int = 256, seed: int = 0, edges=EDGES, precision: str = "mixed", step_cap: bool = True) -> list:
+    """Parameters of ``count`` solves drawn with numpy's PCG64 generator from ``seed``;
+    ``step_cap``: the PT step from :func:`capped_cfl` instead of the reference's CFL."""
     rng = np.random.default_rng(seed)
     cases = []
     for i in range(count):
@@ -44,6 +62,10 @@ def sweep_cases(count: int = 256, seed: int = 0, edges=EDGES, precision: str = "
         else:
             p = default_params("cartesian", n1=n[0], n2=n[1], n3=n[2], bc="diapir", sh=s, vr=1.0 / ratio, incl_linear=1,
                                precision=precision, **rheo)
+        if step_cap:
+            cfl = 1.0 / (2.0 + 4.5 * math.log10(p.vr))
+            base = p.vpdt / cfl if p.vpdt > 0 else p.l1 / (p.n1 - 1)  # the spacing the reference's step scales
+            p.vpdt = base * capped_cfl(p.vr)
         cases.append(p)
     return cases
 
@@ -77,4 +99,4 @@ def run(cases: list, opts, threads: int = 0, autotune: bool = True, serial: bool
             sv.close()
 
 
-__all__ = ["sweep_cases", "run", "make_opts", "EDGES", "GEOMETRIES"]
+__all__ = ["sweep_cases", "capped_cfl", "run", "make_opts", "EDGES", "GEOMETRIES"]

@@ -518,29 +518,37 @@ def run_ours(args) -> None:
         bo = S.make_opts(tol=1e-8, maxiter=args.batch_budget, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=30,
                          inner_max=args.batch_budget, warm_tol=0.0)
         rb = B.run(cases, bo, threads=args.batch_threads, autotune=bool(args.batch_autotune))
-        rs = B.run(cases, bo, serial=True, autotune=bool(args.batch_autotune))
+        # the serial reference: every stride-th case solved alone, one after another
+        stride = max(1, args.batch // args.batch_serial) if args.batch_serial > 0 else 1
+        sub = list(range(0, args.batch, stride))
+        rs = B.run([cases[i] for i in sub], bo, serial=True, autotune=bool(args.batch_autotune))
         cells = [c.n1 * c.n2 * c.n3 for c in cases]
 
-        def leg(r):
+        def leg(r, idx):
             conv = [x for x in r["results"] if x.converged]
-            work = sum(n * x.iters for n, x in zip(cells, r["results"]))  # cell sweeps done
-            return {"wall_s": round(r["wall_s"], 3), "converged": len(conv),
+            work = sum(cells[i] * x.iters for i, x in zip(idx, r["results"]))  # cell sweeps done
+            return {"solves": len(idx), "wall_s": round(r["wall_s"], 3), "converged": len(conv),
                     "converged_solves_per_s": round(len(conv) / r["wall_s"], 3),
                     "cell_sweeps_per_s": round(work / r["wall_s"], 1),
                     "teff_gbs": round(work * 26 * 4 / r["wall_s"] / 1e9, 1)}
 
-        lb, ls = leg(rb), leg(rs)
-        same = all((a.status, a.iters, a.outer) == (b.status, b.iters, b.outer) for a, b in zip(rb["results"], rs["results"]))
+        lb, ls = leg(rb, range(args.batch)), leg(rs, sub)
+        same = all((rb["results"][i].status, rb["results"][i].iters, rb["results"][i].outer) == (b.status, b.iters, b.outer)
+                   for i, b in zip(sub, rs["results"]))
         lockstep = len({x.seconds for x in rb["results"]}) == 1
         batch_info = {"solves": args.batch, "edges": list(edges), "budget_sweeps": args.batch_budget, "batch": lb, "serial": ls,
-                      "speedup_vs_serial": round(rs["wall_s"] / rb["wall_s"], 2),
+                      "speedup_vs_serial": (round(lb["converged_solves_per_s"] / ls["converged_solves_per_s"], 2)
+                                            if ls["converged_solves_per_s"] > 0 else None),
+                      "speedup_basis": "converged solves per second, batch (all solves) over serial (every "
+                                       f"{stride}-th solve alone)",
                       "mode": "lockstep (one launch per sweep over all solves' blocks, graph-replayed rounds)" if lockstep
                               else "host threads, one stream per solve",
-                      "batch_equals_serial": same, "statuses": {str(k): sum(1 for x in rb["results"] if x.status == k)
+                      "batch_equals_serial_subset": same, "statuses": {str(k): sum(1 for x in rb["results"] if x.status == k)
                                                                for k in sorted({x.status for x in rb["results"]})},
                       "cases": "seed-0 draw: edge per axis from the list, geometry cycled sph/cyl/cart, n in 1..4, "
                                "viscosity ratio log-U[1e-4,1e-1], stress ratio U[0,1]; mixed precision to residual 1e-8 "
-                               "or the sweep budget" + ("; autotuned chunk per size" if args.batch_autotune else "")}
+                               "or the sweep budget; PT step at most CFL(1e2)·sqrt(1e2/vr) of the spacing"
+                               + ("; autotuned chunk per size" if args.batch_autotune else "")}
 
     if rank != 0:
         return
@@ -619,6 +627,8 @@ def main():
     ap.add_argument("--batch-budget", type=int, default=4000, help="sweep budget per batched solve")
     ap.add_argument("--batch-autotune", type=int, default=0, help="autotune the sweep chunk per grid size first")
     ap.add_argument("--batch-threads", type=int, default=16)
+    ap.add_argument("--batch-serial", type=int, default=32,
+                    help="solves of the serial reference (every batch/this-th case; 0: all)")
     ap.add_argument("--plateau-sweeps", type=int, default=200,
                     help="sweeps timed on the 511x255x255 elliptical-plateau grid (0: skip)")
     ap.add_argument("--plateau-top", default="free_surface", choices=["free_surface", "sticky_air"])

@@ -14,9 +14,9 @@ velocity node between two cells whose ηSM differ by vr takes the mean of their 
 (compute_V!, SphericalStokes_diapir.jl:315-327), about vr/2 times the step that the
 stiffer cell's pressure tolerates, so the local Courant number is CFL·sqrt(vr/2): 0.64
 at vr = 10^2, 1.4 at 10^3 and 3.5 at 10^4.  Draws above 10^2 then diverge within a few
-hundred iterations (plain FP64 PT as well as the mixed solve).  ``step_cap`` limits the
-step to 0.64/sqrt(vr/2) of the spacing, the Courant number the reference's own choice
-has at vr = 10^2.  The PT step does not change the discrete equations, only how fast
+hundred iterations (plain FP64 PT as well as the mixed solve).  ``step_cap`` keeps the
+local Courant number at the value the reference's choice has at vr = 10^2: the step is
+at most CFL(10^2)·sqrt(10^2/vr) of the spacing.  The PT step does not change the discrete equations, only how fast
 (and whether) the iteration reaches their solution.  The stress ratio s sets the far-field normal
 stresses (0, +s/2, -s/2) on the spherical sector and the cylindrical faces; the
 Cartesian scheme has no deviatoric normal stresses to load, so there s is the
@@ -36,8 +36,8 @@ GEOMETRIES = ("spherical", "cylindrical", "cartesian")
 
 
 def capped_cfl(vr: float) -> float:
-    """The reference's CFL = 1/(2 + 4.5 log10 vr), limited to 0.64/sqrt(vr/2) (module docstring)."""
-    return min(1.0 / (2.0 + 4.5 * math.log10(vr)), 0.64 / math.sqrt(0.5 * vr))
+    """The reference's CFL = 1/(2 + 4.5 log10 vr), limited to CFL(10^2)·sqrt(10^2/vr) (module docstring)."""
+    return min(1.0 / (2.0 + 4.5 * math.log10(vr)), (1.0 / 11.0) * math.sqrt(100.0 / vr))
 
 
 def sweep_cases(count: int = 256, seed: int = 0, edges=EDGES, precision: str = "mixed", step_cap: bool = True) -> list:

@@ -22,6 +22,20 @@ def test_sweep_cases_follow_the_distribution():
     assert all(a.n1 == b.n1 and a.vr == b.vr and a.sig_bc[1] == b.sig_bc[1] and a.sh == b.sh for a, b in zip(cases, again))
 
 
+def test_batch_step_cap():
+    """the reference's CFL up to a viscosity ratio of 1e2, then CFL(1e2) sqrt(1e2/vr)"""
+    ref = lambda vr: 1.0 / (2.0 + 4.5 * np.log10(vr))
+    for vr in (1.5, 10.0, 99.0):
+        assert B.capped_cfl(vr) == ref(vr)
+    for vr in (1e3, 1e4):
+        assert B.capped_cfl(vr) == pytest.approx(np.sqrt(100.0 / vr) / 11.0, rel=1e-15) and B.capped_cfl(vr) < ref(vr)
+    for c, r in zip(B.sweep_cases(30, seed=0), B.sweep_cases(30, seed=0, step_cap=False)):
+        if c.geometry == 0:
+            assert c.vpdt == pytest.approx(r.vpdt * B.capped_cfl(c.vr) / ref(c.vr), rel=1e-12)
+        else:  # the library's own step, dr CFL, is set at create time for these
+            assert r.vpdt == 0.0 and c.vpdt == pytest.approx(c.l1 / (c.n1 - 1) * B.capped_cfl(c.vr), rel=1e-12)
+
+
 def _small_cases(precision):
     return [
         S.sector_params((23, 17, 15), bc="stress", rheology="edot_power_relax", n_exp=3.0, relax=0.5, edot_bg=0.25,

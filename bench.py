@@ -228,6 +228,30 @@ def cpu_time_to_tol(n: int, tol: float = 1e-8, check: int = 1000, max_iters: int
                      f"{check} iterations (the reference's Threads backend is absent: oracle port of its kernels)"}
 
 
+def linear_time_to_tolerance(n: int, tol: float = 1e-8) -> dict:
+    """configs[0] on the GPU: the setup of ``cpu_time_to_tol`` (linear free-slip n^3 sector, the
+    reference's PT step) to FP64 residual ``tol``, as plain FP64 PT and as the mixed solve."""
+    import sphericalstokes_gb300 as S
+
+    info: dict = {"n": n, "tol": tol, "setup": "linear free-slip sector, inclusion η 1e-3 Δρ -1 r 0.1, reference PT step"}
+    for prec in ("fp64", "mixed"):
+        p = workload_params(n, prec)
+        S.set_params(p, bc="free_slip", rheology="linear", n_exp=1.0, sig_bc=(0.0, 0.0, 0.0))
+        with S.Solver(p) as sv:
+            if prec == "fp64":
+                r = sv.solve(tol=tol, maxiter=5_000_000, nout=1000, criterion="residual")
+            else:
+                r = sv.solve(tol=tol, maxiter=5_000_000, nout=100, criterion="residual", inner_rtol=1e-2, max_outer=200,
+                             inner_max=300_000, warm_tol=0.0)
+            info[prec] = {"seconds": round(r.seconds, 3), "iterations": r.iters, "residual": r.residual, "converged": r.converged}
+            info[prec + "_V"] = [sv.get(f) for f in ("V1", "V2", "V3")]
+    vmax = max(float(abs(v).max()) for v in info["fp64_V"])
+    info["rel_velocity_error_mixed_vs_fp64"] = max(float(abs(a - b).max()) for a, b in zip(info.pop("mixed_V"), info.pop("fp64_V"))) / vmax
+    if info["mixed"]["converged"] and info["fp64"]["converged"]:
+        info["speedup_mixed_vs_fp64"] = round(info["fp64"]["seconds"] / info["mixed"]["seconds"], 2)
+    return info
+
+
 def run_reference(args) -> None:
     """The reference's CPU implementation of the path (the oracle port of its kernels, all host
     threads) on the same workload.  A step is one FP64 PT iteration over a sample of the grid:
@@ -472,6 +496,9 @@ def run_ours(args) -> None:
 
     if args.solve_n:
         solve_info = time_to_tolerance(args)
+    linear_info = None
+    if args.linear_solve_n:
+        linear_info = linear_time_to_tolerance(args.linear_solve_n)
     # plain FP64 PT (one kernel per reference step) on the same workload: its time per iteration,
     # the per-iteration baseline of the mixed-precision solve's FP32 sweep
     fp64_info = None
@@ -572,6 +599,8 @@ def run_ours(args) -> None:
         line["e2e"] = e2e
     if solve_info:
         line["time_to_tol"] = solve_info
+    if linear_info:
+        line["linear_time_to_tol"] = linear_info
     if batch_info:
         line["batch"] = batch_info
     if plateau_info:
@@ -606,6 +635,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0, help="target length of the --impl reference run")
+    ap.add_argument("--linear-solve-n", type=int, default=0,
+                    help="configs[0] on the GPU: the linear free-slip n^3 sector to residual 1e-8, FP64 PT and mixed (0: skip)")
     ap.add_argument("--cpu-solve-n", type=int, default=0,
                     help="--impl reference: also iterate the linear n^3 sector (configs[0]) to residual 1e-8 on the CPU")
     ap.add_argument("--prep-sweeps", type=int, default=500)
@@ -624,7 +655,7 @@ def main():
     ap.add_argument("--batch", type=int, default=256, help="batched-solve leg: number of solves (0: skip)")
     ap.add_argument("--batch-edges", default="31,47",
                     help="grid edges the batched solves draw from (the full sweep: 31,47,63,79,95)")
-    ap.add_argument("--batch-budget", type=int, default=4000, help="sweep budget per batched solve")
+    ap.add_argument("--batch-budget", type=int, default=100_000, help="sweep budget per batched solve")
     ap.add_argument("--batch-autotune", type=int, default=0, help="autotune the sweep chunk per grid size first")
     ap.add_argument("--batch-threads", type=int, default=16)
     ap.add_argument("--batch-serial", type=int, default=32,

@@ -369,9 +369,8 @@ int sph_save(void* ctx, const char* dir, int32_t num, double tol, double runtime
  * It allocates no memory: its reduction slots are a static device array of
  * 2 * SPH_NOALLOC_MAX_ARRAYS * 8 bytes shared by every call, so calls that overlap on
  * the GPU race.  The first call on a device looks the array up (cudaGetSymbolAddress)
- * with that device current; make that first call before any stream capture.  The address
- * is kept for the life of the process, so no call may follow a cudaDeviceReset of that
- * device.  A NaN in v[i] or v_old[i] makes *err NaN (Julia's maximum propagates NaN). */
+ * with that device current.  The address is kept for the life of the process, so no call
+ * may follow a cudaDeviceReset of that device.  A NaN in v[i] or v_old[i] makes *err NaN (Julia's maximum propagates NaN). */
 #define SPH_NOALLOC_MAX_ARRAYS 8
 int sph_check_err_noalloc(int32_t m, const double* const* v, const double* const* v_old, const int64_t* count, double* err,
                           void* stream);

@@ -16,7 +16,9 @@ stiffer cell's pressure tolerates, so the local Courant number is CFL·sqrt(vr/2
 at vr = 10^2, 1.4 at 10^3 and 3.5 at 10^4.  Draws above 10^2 then diverge within a few
 hundred iterations (plain FP64 PT as well as the mixed solve).  ``step_cap`` keeps the
 local Courant number at the value the reference's choice has at vr = 10^2: the step is
-at most CFL(10^2)·sqrt(10^2/vr) of the spacing.  The PT step does not change the discrete equations, only how fast
+at most CFL(10^2)·sqrt(10^2/c) of the spacing, c the viscosity contrast of the solve's
+starting state (vr, or 2 vr under the strain-rate law, whose zero-strain-rate viscosity is
+twice the linear one).  The PT step does not change the discrete equations, only how fast
 (and whether) the iteration reaches their solution.  The stress ratio s sets the far-field normal
 stresses (0, +s/2, -s/2) on the spherical sector and the cylindrical faces; the
 Cartesian scheme has no deviatoric normal stresses to load, so there s is the
@@ -65,7 +67,10 @@ def sweep_cases(count: int = 256, seed: int = 0, edges=EDGES, precision: str = "
         if step_cap:
             cfl = 1.0 / (2.0 + 4.5 * math.log10(p.vr))
             base = p.vpdt / cfl if p.vpdt > 0 else p.l1 / (p.n1 - 1)  # the spacing the reference's step scales
-            p.vpdt = base * capped_cfl(p.vr)
+            # the strain-rate law starts from twice the linear viscosity (η_t = 2/(1/η_ini + 1/η_PL)
+            # at zero strain rate) over the linear inclusion: the contrast is 2 vr
+            contrast = p.vr * (2.0 if n_exp > 1 else 1.0)
+            p.vpdt = base * min(cfl, capped_cfl(contrast))
         cases.append(p)
     return cases
 

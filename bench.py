@@ -518,12 +518,15 @@ def run_ours(args) -> None:
         with PL.ellipse_solver(ep, "mixed") as sv:
             sv.sweep(args.warmup)
             ms = sv.sweep(args.plateau_sweeps)
-            r_solve = None
-            if args.plateau_solve_sweeps > 0:  # a budget-bounded mixed solve from the initial state
-                sv.sweep_apply()
+        r_solve = None
+        if args.plateau_solve_sweeps > 0:  # a budget-bounded mixed solve from the initial state
+            p0 = ep.params("mixed")
+            step = args.plateau_step * p0.l1 / (p0.n1 - 1) / (2.0 + 4.5 * math.log10(p0.vr))  # x the library's dr CFL
+            with PL.ellipse_solver(ep, "mixed", vpdt=step) as sv:
                 r0 = sv.residual()["err"]
-                r_solve = sv.solve(tol=1e-8, maxiter=args.plateau_solve_sweeps, nout=100, criterion="residual", inner_rtol=0.1,
-                                   max_outer=1000, inner_max=60000)
+                r_solve = sv.solve(tol=1e-8, maxiter=args.plateau_solve_sweeps, nout=100, criterion="residual", inner_rtol=1e-2,
+                                   max_outer=1000, inner_max=100_000, hist_cap=10_000)
+                ms_hist = sv.history_ms()
         cells = ep.nr * ep.nth * ep.nph
         plateau_info = {"grid": [ep.nr, ep.nth, ep.nph], "sweeps": args.plateau_sweeps, "top": ep.top,
                         "ms_per_sweep": round(ms / args.plateau_sweeps, 4),
@@ -534,7 +537,9 @@ def run_ours(args) -> None:
                                    else "20 km sticky air") + "; FP32 correction sweeps")}
         if r_solve is not None:
             plateau_info["solve"] = {"sweeps": r_solve.iters, "outer": r_solve.outer, "seconds": round(r_solve.seconds, 2),
-                                     "initial_residual": r0, "residual": r_solve.residual, "status": r_solve.status}
+                                     "initial_residual": r0, "residual": r_solve.residual, "status": r_solve.status,
+                                     "pt_step": f"{args.plateau_step:g} x the reference's (dr CFL), dmp {ep.dmp:g}",
+                                     "curve_s_residual": _curve(ms_hist, r_solve.hist_err[:len(ms_hist)])}
 
     batch_info = None
     if args.batch > 0:
@@ -663,6 +668,8 @@ def main():
     ap.add_argument("--plateau-sweeps", type=int, default=200,
                     help="sweeps timed on the 511x255x255 elliptical-plateau grid (0: skip)")
     ap.add_argument("--plateau-top", default="free_surface", choices=["free_surface", "sticky_air"])
+    ap.add_argument("--plateau-step", type=float, default=0.25,
+                    help="PT step of the plateau solve, as a multiple of the reference's dr CFL")
     ap.add_argument("--plateau-solve-sweeps", type=int, default=0,
                     help="sweep budget of a mixed solve of the plateau from its initial state (0: skip)")
     args = ap.parse_args()

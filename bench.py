@@ -499,6 +499,16 @@ def run_ours(args) -> None:
     linear_info = None
     if args.linear_solve_n:
         linear_info = linear_time_to_tolerance(args.linear_solve_n)
+    adjoint_info = None
+    if args.adjoint_n:
+        from sphericalstokes_gb300 import adjoint as A
+
+        with S.Solver(workload_params(args.adjoint_n, "fp64")) as sv:
+            adjoint_info = A.fd_check(sv, directions=args.adjoint_dirs, seed=0)
+        adjoint_info = {"n": args.adjoint_n, "objective": "1/2 sum (V_r - V_obs)^2 on the top interior face; V_obs from "
+                        "a forward solve with log eta_ini + N(0, 0.1^2) per cell (seed 0)",
+                        "parameters": "log eta_ini per cell, n, rho per cell; central differences eps 1e-4, forward solves "
+                        "to FP64 residual 1e-12", **adjoint_info}
     # plain FP64 PT (one kernel per reference step) on the same workload: its time per iteration,
     # the per-iteration baseline of the mixed-precision solve's FP32 sweep
     fp64_info = None
@@ -606,6 +616,8 @@ def run_ours(args) -> None:
         line["time_to_tol"] = solve_info
     if linear_info:
         line["linear_time_to_tol"] = linear_info
+    if adjoint_info:
+        line["adjoint_fd"] = adjoint_info
     if batch_info:
         line["batch"] = batch_info
     if plateau_info:
@@ -640,6 +652,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=90.0, help="target length of the --impl reference run")
+    ap.add_argument("--adjoint-n", type=int, default=0,
+                    help="adjoint gradient of the n^3 workload against central differences (0: skip)")
+    ap.add_argument("--adjoint-dirs", type=int, default=16, help="seeded random directions of that check")
     ap.add_argument("--linear-solve-n", type=int, default=0,
                     help="configs[0] on the GPU: the linear free-slip n^3 sector to residual 1e-8, FP64 PT and mixed (0: skip)")
     ap.add_argument("--cpu-solve-n", type=int, default=0,

@@ -165,3 +165,12 @@ def test_power_law_gradients_match_central_differences():
         fd = (J_at(rho=rho0 + eps * d) - J_at(rho=rho0 - eps * d)) / (2 * eps)
         ad = float(np.sum(grad["drho"] * d))
         assert abs(fd - ad) <= 1e-5 * abs(fd), ("rho", fd, ad)
+
+
+def test_fd_check_of_the_power_law_misfit():
+    """adjoint.fd_check (the bench's configs[4]-style leg) on a small grid: the adjoint gradient along
+    seeded random directions in (log η_ini per cell, n, ρ per cell) equals central differences"""
+    with S.Solver(_law_params()) as sv:
+        r = A.fd_check(sv, directions=3, seed=1)
+    assert len(r["directions"]) == 3 and r["forward_solves"] == 2 + 2 * 3
+    assert r["max_rel_diff"] <= 1e-5, r["directions"]

@@ -203,14 +203,30 @@ def cpu_baseline(n: int, seconds: float = 15.0, threads: int | None = None) -> d
             "sample": f"{it} FP64 PT iterations of the {n}^3 workload ({dt * 1e3:.1f} ms each)"}
 
 
+def linear_reference_params(n: int):
+    """configs[0] built without the library: the n^3 sector with linear viscosity and free slip
+    on all faces (the reference's diapir step and inclusion), as ``linear_params`` gives the library."""
+    p = reference_params(n)
+    p.bc, p.rheology, p.n_exp, p.sig_bc = 1, 0, 1.0, (0.0, 0.0, 0.0)
+    return p
+
+
+def linear_params(n: int, precision: str):
+    """configs[0] for the library: the workload's sector with linear viscosity and free slip."""
+    import sphericalstokes_gb300 as S
+
+    p = workload_params(n, precision)
+    S.set_params(p, bc="free_slip", rheology="linear", n_exp=1.0, sig_bc=(0.0, 0.0, 0.0))
+    return p
+
+
 def cpu_time_to_tol(n: int, tol: float = 1e-8, check: int = 1000, max_iters: int = 5_000_000) -> dict:
     """configs[0] on the CPU: plain FP64 PT of the oracle port (all host threads) on the n^3 spherical
     sector, linear viscosity (inclusion 1e-3, Δρ = -1), free slip on all faces, the reference's PT
     step, iterated to FP64 residual `tol` (checked every `check` iterations)."""
     import oracle
 
-    p = reference_params(n)
-    p.bc, p.rheology, p.n_exp, p.sig_bc = 1, 0, 1.0, (0.0, 0.0, 0.0)
+    p = linear_reference_params(n)
     o = oracle.Sph.from_params(p)
     t0 = time.perf_counter()
     it, err, hist = 0, float("inf"), []
@@ -235,8 +251,7 @@ def linear_time_to_tolerance(n: int, tol: float = 1e-8) -> dict:
 
     info: dict = {"n": n, "tol": tol, "setup": "linear free-slip sector, inclusion η 1e-3 Δρ -1 r 0.1, reference PT step"}
     for prec in ("fp64", "mixed"):
-        p = workload_params(n, prec)
-        S.set_params(p, bc="free_slip", rheology="linear", n_exp=1.0, sig_bc=(0.0, 0.0, 0.0))
+        p = linear_params(n, prec)
         with S.Solver(p) as sv:
             if prec == "fp64":
                 r = sv.solve(tol=tol, maxiter=5_000_000, nout=1000, criterion="residual")

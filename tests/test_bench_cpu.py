@@ -28,6 +28,17 @@ def test_reference_workload_equals_library_workload(n):
     assert tuple(ref.sig_bc) == tuple(lib.sig_bc)
 
 
+@pytest.mark.parametrize("n", [23, 63])
+def test_linear_case_is_the_same_on_both_sides(n):
+    """configs[0]: the GPU leg's parameters equal those the oracle port iterates on the CPU"""
+    lib = bench.linear_params(n, "fp64")
+    ref = bench.linear_reference_params(n)
+    for k in KEYS:
+        assert getattr(ref, k) == pytest.approx(getattr(lib, k), rel=1e-15, abs=0.0), k
+    assert tuple(ref.sig_bc) == tuple(lib.sig_bc) == (0.0, 0.0, 0.0)
+    assert lib.bc == 1 and lib.rheology == 0
+
+
 def test_reference_sample_keeps_the_spacing():
     full, _ = bench.reference_workload(31)
     sample, _ = bench.reference_workload(31, 9)

@@ -513,7 +513,7 @@ def run_ours(args) -> None:
                "copy_share": round((t_up + t_down) / wall, 3),
                "step": f"upload 8 fields from pinned host memory, {r.iters} mixed-precision sweeps + FP64 residual, "
                        "download V and P into pinned host memory (one call chain); h2d_gbs / d2h_gbs: host-timed "
-                       "rates of the field calls (copy + repack kernel + FP32 mirror)"}
+                       "rates of the field calls (one contiguous copy each plus the repack kernel into the padded box)"}
 
     if args.solve_n:
         solve_info = time_to_tolerance(args)

@@ -204,7 +204,7 @@ def cpu_baseline(n: int, seconds: float = 15.0, threads: int | None = None) -> d
 
 
 def linear_reference_params(n: int):
-    """configs[0] built without the library: the n^3 sector with linear viscosity and free slip
+    """The linear case built without the library: the n^3 sector with linear viscosity and free slip
     on all faces (the reference's diapir step and inclusion), as ``linear_params`` gives the library."""
     p = reference_params(n)
     p.bc, p.rheology, p.n_exp, p.sig_bc = 1, 0, 1.0, (0.0, 0.0, 0.0)
@@ -212,7 +212,7 @@ def linear_reference_params(n: int):
 
 
 def linear_params(n: int, precision: str):
-    """configs[0] for the library: the workload's sector with linear viscosity and free slip."""
+    """The linear case for the library: the workload's sector with linear viscosity and free slip."""
     import sphericalstokes_gb300 as S
 
     p = workload_params(n, precision)
@@ -221,7 +221,7 @@ def linear_params(n: int, precision: str):
 
 
 def cpu_time_to_tol(n: int, tol: float = 1e-8, check: int = 1000, max_iters: int = 5_000_000) -> dict:
-    """configs[0] on the CPU: plain FP64 PT of the oracle port (all host threads) on the n^3 spherical
+    """The linear 63^3-style case on the CPU: plain FP64 PT of the oracle port (all host threads) on the n^3 spherical
     sector, linear viscosity (inclusion 1e-3, Δρ = -1), free slip on all faces, the reference's PT
     step, iterated to FP64 residual `tol` (checked every `check` iterations)."""
     import oracle
@@ -245,7 +245,7 @@ def cpu_time_to_tol(n: int, tol: float = 1e-8, check: int = 1000, max_iters: int
 
 
 def linear_time_to_tolerance(n: int, tol: float = 1e-8) -> dict:
-    """configs[0] on the GPU: the setup of ``cpu_time_to_tol`` (linear free-slip n^3 sector, the
+    """The linear case on the GPU: the setup of ``cpu_time_to_tol`` (linear free-slip n^3 sector, the
     reference's PT step) to FP64 residual ``tol``, as plain FP64 PT and as the mixed solve."""
     import sphericalstokes_gb300 as S
 
@@ -677,9 +677,9 @@ def main():
                     help="adjoint gradient of the n^3 workload against central differences (0: skip)")
     ap.add_argument("--adjoint-dirs", type=int, default=16, help="seeded random directions of that check")
     ap.add_argument("--linear-solve-n", type=int, default=0,
-                    help="configs[0] on the GPU: the linear free-slip n^3 sector to residual 1e-8, FP64 PT and mixed (0: skip)")
+                    help="the linear free-slip n^3 sector to residual 1e-8 on the GPU, FP64 PT and mixed (0: skip)")
     ap.add_argument("--cpu-solve-n", type=int, default=0,
-                    help="--impl reference: also iterate the linear n^3 sector (configs[0]) to residual 1e-8 on the CPU")
+                    help="--impl reference: also iterate the linear free-slip n^3 sector to residual 1e-8 on the CPU")
     ap.add_argument("--prep-sweeps", type=int, default=500)
     ap.add_argument("--max-sweeps", type=int, default=2_000_000)
     ap.add_argument("--inner-rtol", type=float, default=1e-2)

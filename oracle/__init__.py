@@ -3,7 +3,7 @@
 ctypes wrapper of ``oracle/_build/liboracle.so``, the FP64 CPU restatement of
 the reference's PT kernels (``oracle/oracle.cpp``).  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU baseline / reference arm
-use it, as the checker; the product library never calls it.
+use it, as the reference the GPU results are compared with; the product library never calls it.
 
 Arrays are numpy float64 in the reference's layout: Fortran order, the sizes of
 the scripts' ``@zeros`` calls, ``A[i,j,k]`` = Julia ``A[i+1,j+1,k+1]``.

@@ -168,7 +168,7 @@ def test_power_law_gradients_match_central_differences():
 
 
 def test_fd_check_of_the_power_law_misfit():
-    """adjoint.fd_check (the bench's configs[4]-style leg) on a small grid: the adjoint gradient along
+    """adjoint.fd_check (the bench's gradient-check leg) on a small grid: the adjoint gradient along
     seeded random directions in (log η_ini per cell, n, ρ per cell) equals central differences"""
     with S.Solver(_law_params()) as sv:
         r = A.fd_check(sv, directions=3, seed=1)

@@ -30,7 +30,7 @@ def test_reference_workload_equals_library_workload(n):
 
 @pytest.mark.parametrize("n", [23, 63])
 def test_linear_case_is_the_same_on_both_sides(n):
-    """configs[0]: the GPU leg's parameters equal those the oracle port iterates on the CPU"""
+    """the linear free-slip case: the GPU leg's parameters equal those the oracle port iterates on the CPU"""
     lib = bench.linear_params(n, "fp64")
     ref = bench.linear_reference_params(n)
     for k in KEYS:

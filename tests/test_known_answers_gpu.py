@@ -49,7 +49,7 @@ def test_power_law_with_n_one_returns_the_initial_viscosity():
 
 
 def test_centred_inclusion_is_mirror_symmetric():
-    """the sphere of configs[0] is centred at θ = π/2, φ = 0: P, V_r mirror-symmetric, V_θ odd in θ, V_φ odd in φ"""
+    """the sector's inclusion is centred at θ = π/2, φ = 0: P, V_r mirror-symmetric, V_θ odd in θ, V_φ odd in φ"""
     p = S.sector_params((21, 19, 17), bc="free_slip", rheology="linear")
     with S.Solver(p) as sv:
         sv.step(300)
@@ -65,7 +65,7 @@ def test_centred_inclusion_is_mirror_symmetric():
 
 
 def test_converged_linear_sphere_matches_the_oracle():
-    """configs[0] (free slip, linear, centred inclusion) on a small grid to FP64 residual 1e-8,
+    """the linear free-slip sector (centred inclusion) on a small grid to FP64 residual 1e-8,
     then the oracle for the same number of iterations"""
     p = S.sector_params((19, 17, 15), bc="free_slip", rheology="linear")
     with S.Solver(p) as sv:

@@ -618,7 +618,8 @@ def run_ours(args) -> None:
     line = {
         "metric": METRIC, "value": out["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": out["ms_per_step"], "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32 sweeps + fp64 residual/correction", "data": "synthetic",
+        "vs_baseline": None, "dtype": "f32", "precision": "FP32 sweeps inside FP64 defect correction (residual, update, norms in FP64)",
+        "data": "synthetic",
         "config": workload_config(n),
         "ms_per_iteration": round(ms_step_max, 5), "word_bytes": word,
         "iteration": "one FP32 PT sweep of the FP32+FP64 defect-correction solve",

@@ -59,3 +59,20 @@ def test_reference_arm_does_not_map_the_product_library():
     assert line["impl"] == "reference" and line["config"] == bench.workload_config(23)
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
     assert line["ms_per_iteration"] > 0 and line["word_bytes"] == 8
+
+
+def test_time_to_and_curve_helpers():
+    ms = [10.0, 20.0, 30.0, 40.0]
+    err = [1.0, 0.5, 0.05, 0.001]
+    assert bench._time_to(ms, err, 0.5) == pytest.approx(0.020)
+    assert bench._time_to(ms, err, 0.01) == pytest.approx(0.040)
+    assert bench._time_to(ms, err, 1e-9) is None
+    c = bench._curve(ms, err, keep=3)
+    assert c[0] == [0.01, 1.0] and c[-1] == [0.04, 0.001] and len(c) == 3
+
+
+def test_pt_parameters_states_the_solve_s_own_values():
+    p = bench.workload_params(63, "fp64", tuned=True)
+    assert bench.pt_parameters(p, 63).startswith("pseudo-step 2x") and "dmp 3" in bench.pt_parameters(p, 63)
+    q = bench.workload_params(63, "fp64", dmp=3.5)
+    assert "pseudo-step 1x" in bench.pt_parameters(q, 63) and "dmp 3.5" in bench.pt_parameters(q, 63)
